@@ -1,0 +1,196 @@
+// Test-infrastructure driver around the reference implementation's own
+// short-range MD path.  It is linked against the reference's objects (built
+// from its sources by the Makefile beside it) and only prints what the
+// reference computes; it implements no physics of its own.
+//
+// Modes (all values printed with 17 significant digits):
+//   forces <file.inp> <rc> <rcLJ> <periodic 0|1>
+//       One force evaluation, set up the way the reference's unit tests do
+//       (ParticleContainerFactory::createInitializedParticleContainer): read the
+//       ASCII phase space, build LinkedCells(cutoff = rc), update, optionally
+//       run the serial periodic exchange (leaving particles + halo copies),
+//       build the SoA caches, traverse with VectorizedCellProcessor and call
+//       calcFM on every inner molecule.  Also traverses with the FlopCounter.
+//   steps <file.inp> <rc> <rcLJ> <dt> <nsteps>
+//       NVE Leapfrog steps with the periodic halo, in the order of the
+//       reference's Simulation::simulateOneTimestep (thermostat off, no
+//       long-range correction).  Prints per-step Upot, virial, 2*Ukin_trans and
+//       2*Ukin_rot and the final per-molecule state.
+//
+// Output records:
+//   N <count>
+//   GRID <cells per dim incl. halo x3> <cell length x3>
+//   UPOT <local Upot>   VIRIAL <local virial>
+//   COUNTS <molecule distances> {<kernel calls> <macro calls>} x 7 potentials
+//   STEP <k> <Upot> <virial> <summv2> <sumIw2>
+//   MOL <id> <comp> <cell> r[3] v[3] q[4] L[3] F[3] M[3] Vi[3]
+
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include <iostream>
+#include <memory>
+
+#include "Domain.h"
+#include "Simulation.h"
+#include "ensemble/EnsembleBase.h"
+#include "integrators/Leapfrog.h"
+#include "io/ASCIIReader.h"
+#include "molecules/Molecule.h"
+#include "parallel/DomainDecompBase.h"
+#include "particleContainer/LinkedCells.h"
+#include "particleContainer/adapter/VectorizedCellProcessor.h"
+#include "particleContainer/adapter/vectorization/SIMD_TYPES.h"
+#include "utils/Logger.h"
+// The per-potential call counters of FlopCounter are private members; they are
+// read here (not modified) to report the reference's own pair counts.
+#define private public
+#include "particleContainer/adapter/FlopCounter.h"
+#undef private
+
+static_assert(VCP_VEC_TYPE == VCP_NOVEC, "golden vectors come from the scalar kernel path");
+
+namespace {
+
+struct Setup {
+	Domain* domain = nullptr;
+	DomainDecompBase* dd = nullptr;
+	LinkedCells* lc = nullptr;
+	ASCIIReader reader;
+};
+
+void load(Setup& s, const std::string& file, double rc, double rcLJ) {
+	new Simulation();  // assigns global_simulation
+	s.domain = global_simulation->getDomain();
+	s.dd = &global_simulation->domainDecomposition();
+	global_simulation->setcutoffRadius(rc);
+	global_simulation->setLJCutoff(rcLJ);
+	s.reader.setPhaseSpaceHeaderFile(file);
+	s.reader.setPhaseSpaceFile(file);
+	s.reader.readPhaseSpaceHeader(s.domain, 1.0);
+	double bmin[3], bmax[3];
+	for (int d = 0; d < 3; ++d) {
+		bmin[d] = s.dd->getBoundingBoxMin(d, s.domain);
+		bmax[d] = s.dd->getBoundingBoxMax(d, s.domain);
+	}
+	s.lc = new LinkedCells(bmin, bmax, rc);
+	s.reader.readPhaseSpace(s.lc, s.domain, s.dd);
+	s.lc->deleteOuterParticles();
+	s.lc->update();
+}
+
+void printGrid(const Setup& s) {
+	double bmin[3], bmax[3];
+	for (int d = 0; d < 3; ++d) {
+		bmin[d] = s.lc->getBoundingBoxMin(d);
+		bmax[d] = s.lc->getBoundingBoxMax(d);
+	}
+	const double* cl = s.lc->getCellLength();
+	int n[3];
+	for (int d = 0; d < 3; ++d) n[d] = (int)((bmax[d] - bmin[d]) / cl[d] + 0.5) + 2;
+	std::printf("GRID %d %d %d %.17g %.17g %.17g\n", n[0], n[1], n[2], cl[0], cl[1], cl[2]);
+}
+
+void printMolecules(Setup& s) {
+	struct Row { unsigned long id; std::vector<double> v; int comp; unsigned long cell; };
+	std::vector<Row> rows;
+	for (auto m = s.lc->iterator(ParticleIterator::ONLY_INNER_AND_BOUNDARY); m.isValid(); ++m) {
+		Row r;
+		r.id = m->getID();
+		r.comp = (int)m->componentid();
+		r.cell = s.lc->getCellIndexOfMolecule(&(*m));
+		const Quaternion q = m->q();
+		const double vals[] = {m->r(0), m->r(1), m->r(2), m->v(0), m->v(1), m->v(2),
+							   q.qw(), q.qx(), q.qy(), q.qz(), m->D(0), m->D(1), m->D(2),
+							   m->F(0), m->F(1), m->F(2), m->M(0), m->M(1), m->M(2),
+							   m->Vi(0), m->Vi(1), m->Vi(2)};
+		r.v.assign(vals, vals + sizeof(vals) / sizeof(vals[0]));
+		rows.push_back(r);
+	}
+	std::sort(rows.begin(), rows.end(), [](const Row& a, const Row& b) { return a.id < b.id; });
+	std::printf("N %zu\n", rows.size());
+	for (const Row& r : rows) {
+		std::printf("MOL %lu %d %lu", r.id, r.comp, r.cell);
+		for (double x : r.v) std::printf(" %.17g", x);
+		std::printf("\n");
+	}
+}
+
+int runForces(const std::string& file, double rc, double rcLJ, bool periodic) {
+	Setup s;
+	load(s, file, rc, rcLJ);
+	if (periodic) s.dd->exchangeMolecules(s.lc, s.domain);
+	s.lc->updateMoleculeCaches();
+	s.domain->initParameterStreams(rc, rcLJ);
+
+	FlopCounter flops(rc, rcLJ);
+	s.lc->traverseCells(flops);
+
+	VectorizedCellProcessor vcp(*s.domain, rc, rcLJ);
+	s.lc->traverseCells(vcp);
+	for (auto m = s.lc->iterator(ParticleIterator::ALL_CELLS); m.isValid(); ++m) m->calcFM();
+
+	printGrid(s);
+	std::printf("UPOT %.17g\nVIRIAL %.17g\n", s.domain->getLocalUpot(), s.domain->getLocalVirial());
+	const auto& c = flops._currentCounts;
+	std::printf("COUNTS %.17g", c._moleculeDistances);
+	for (int i = 0; i < FlopCounter::NUM_POTENTIALS; ++i)
+		std::printf(" %.17g %.17g", c._potCounts[i]._numKernelCalls, c._potCounts[i]._numMacroCalls);
+	std::printf("\n");
+	s.lc->deleteOuterParticles();
+	printMolecules(s);
+	return 0;
+}
+
+void forceStep(Setup& s, VectorizedCellProcessor& vcp) {
+	s.lc->traverseCells(vcp);
+	for (auto m = s.lc->iterator(ParticleIterator::ALL_CELLS); m.isValid(); ++m) m->calcFM();
+	s.lc->deleteOuterParticles();
+}
+
+int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nsteps) {
+	Setup s;
+	load(s, file, rc, rcLJ);
+	s.domain->thermostatOff();
+	s.dd->exchangeMolecules(s.lc, s.domain);
+	s.lc->updateMoleculeCaches();
+	s.domain->initParameterStreams(rc, rcLJ);
+	VectorizedCellProcessor vcp(*s.domain, rc, rcLJ);
+	Leapfrog integrator(dt);
+
+	// initial forces, as in Simulation::prepare_start
+	forceStep(s, vcp);
+	printGrid(s);
+	std::printf("STEP 0 %.17g %.17g nan nan\n", s.domain->getLocalUpot(), s.domain->getLocalVirial());
+	for (int k = 1; k <= nsteps; ++k) {
+		integrator.eventNewTimestep(s.lc, s.domain);
+		s.lc->update();
+		s.dd->exchangeMolecules(s.lc, s.domain);
+		s.lc->updateMoleculeCaches();
+		forceStep(s, vcp);
+		integrator.eventForcesCalculated(s.lc, s.domain);
+		const double upot = s.domain->getLocalUpot();
+		const double vir = s.domain->getLocalVirial();
+		s.domain->calculateGlobalValues(s.dd, s.lc, false, 1.0);
+		std::printf("STEP %d %.17g %.17g %.17g %.17g\n", k, upot, vir,
+					2.0 * s.domain->getGlobalUkinTrans(), 2.0 * s.domain->getGlobalUkinRot());
+	}
+	printMolecules(s);
+	return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+	// The reference logs through a global logger that its own main() creates;
+	// send it to stderr so stdout carries only the records above.
+	Log::global_log = std::make_unique<Log::Logger>(Log::Warning, std::shared_ptr<std::ostream>(&std::cerr, [](void*) {}));
+	if (argc >= 6 && std::string(argv[1]) == "forces")
+		return runForces(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atoi(argv[5]) != 0);
+	if (argc >= 7 && std::string(argv[1]) == "steps")
+		return runSteps(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]));
+	std::fprintf(stderr, "usage: %s forces <inp> <rc> <rcLJ> <periodic> | steps <inp> <rc> <rcLJ> <dt> <n>\n", argv[0]);
+	return 2;
+}
