@@ -1,0 +1,161 @@
+/*
+ * ls1gb300.h -- C ABI of the GB300 short-range molecular-dynamics engine.
+ *
+ * One context owns all device buffers and one CUDA stream for one periodic
+ * (or open) box.  The engine replaces, for that box, the reference's
+ *   LinkedCells container (binning, periodic halo, SoA caches),
+ *   VectorizedCellProcessor (site-site LJ-12-6 / charge / dipole /
+ *   quadrupole forces with reaction field, molecule-centre cut-off),
+ *   FullMolecule::calcFM, the Leapfrog integrator and the local Upot/virial
+ *   and kinetic-energy sums.
+ * Every entry point returns MD_OK (0) or an MD_ERR_* code; md_last_error()
+ * gives the message.  Host pointers are borrowed for the duration of the call
+ * only.  Calls on one context must not overlap (the reference calls its
+ * container from the master thread only).  No C++ exception crosses the ABI.
+ *
+ * Reference interfaces replaced (paths relative to the ls1-mardyn tree):
+ *   md_create / md_destroy      LinkedCells::LinkedCells, ~LinkedCells
+ *                               (src/particleContainer/LinkedCells.cpp:38-110)
+ *   md_set_components           Domain::initParameterStreams -> Comp2Param::initialize
+ *                               (src/Domain.cpp:629-631, src/molecules/Comp2Param.cpp:11-202)
+ *                               and the VectorizedCellProcessor constructor's tables
+ *                               (src/particleContainer/adapter/VectorizedCellProcessor.cpp:19-96)
+ *   md_upload_molecules         ParticleContainer::addParticles (ParticleContainer.h:134)
+ *   md_download_molecules       ParticleContainer::iterator (ParticleContainer.h:160)
+ *   md_rebin_and_halo           LinkedCells::update (LinkedCells.cpp:241-355) +
+ *                               DomainDecompBase::exchangeMolecules (DomainDecompBase.cpp:80-114) +
+ *                               LinkedCells::updateMoleculeCaches (LinkedCells.cpp:1097-1107)
+ *   md_get_cell_assignment      LinkedCells::getCellIndexOfMolecule/getCellIndexOfPoint
+ *                               (LinkedCells.cpp:870-923)
+ *   md_compute_forces           LinkedCells::traverseCells(VectorizedCellProcessor)
+ *                               (LinkedCells.cpp:565-575) + Simulation::updateForces
+ *                               (Simulation.cpp:835-845) + VCP::endTraversal (VCP.cpp:122-155)
+ *   md_integrate_pre            Leapfrog::eventNewTimestep (Leapfrog.cpp:38-61)
+ *   md_integrate_post           Leapfrog::eventForcesCalculated (Leapfrog.cpp:32-36, 63-147)
+ *   md_run                      the hot part of Simulation::simulateOneTimestep
+ *                               (Simulation.cpp:1076-1300) for an NVE run
+ */
+#ifndef LS1GB300_H
+#define LS1GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MD_OK 0
+#define MD_ERR_ARG 1          /* invalid argument                                      */
+#define MD_ERR_CUDA 2         /* CUDA runtime error                                    */
+#define MD_ERR_CAPACITY 3     /* a capacity was exceeded; the context re-sizes on retry */
+#define MD_ERR_STATE 4        /* calls out of order (e.g. forces before molecules)     */
+#define MD_ERR_DEVICE 5       /* device status word: NaN, lost molecule, wait limit    */
+#define MD_ERR_UNSUPPORTED 6  /* configuration the engine does not provide             */
+
+#define MD_PREC_FP64 0        /* FP64 pair arithmetic and accumulation                 */
+#define MD_PREC_MIXED 1       /* FP32 pair arithmetic, compensated per-molecule sums,
+                                 FP64 positions, integration and global sums           */
+
+#define MD_NUM_KINDS 7        /* LJ, C-C, C-D, D-D, C-Q, D-Q, Q-Q (FlopCounter order)  */
+
+typedef struct md_ctx md_ctx;
+
+typedef struct {
+    double box_min[3];
+    double box_max[3];
+    double rc;          /* cutoffRadius: molecule-centre cut-off of the electrostatics and
+                           lower bound of the cell edge                                   */
+    double rc_lj;       /* LJ cut-off (molecule centres), <= rc                           */
+    double eps_rf;      /* reaction-field permittivity epsilon_RF                         */
+    int32_t periodic[3];/* 1: serial periodic halo in this dimension; 0: no halo (open)   */
+    int32_t precision;  /* MD_PREC_FP64 or MD_PREC_MIXED                                  */
+    int64_t capacity;   /* molecules to reserve (0: size from the first upload)           */
+    double skin;        /* Verlet skin of the pair-candidate list; 0 rebuilds every step  */
+    int32_t device;     /* CUDA device ordinal                                            */
+    int32_t reserved;
+} md_config;
+
+/* One component (molecule type).  Site tables are row-major doubles:
+ *   lj:         n_lj x 7         x y z m eps sigma shift6
+ *   charge:     n_charge x 5     x y z m q
+ *   dipole:     n_dipole x 7     x y z ex ey ez |mu|
+ *   quadrupole: n_quadrupole x 7 x y z ex ey ez |Q|
+ * Offsets are body-frame; orientation vectors are used as given (the
+ * reference's ASCII reader does not normalise them).  inertia[d] > 0 overrides
+ * the principal moment computed from the massive sites. */
+typedef struct {
+    int32_t n_lj, n_charge, n_dipole, n_quadrupole;
+    const double* lj;
+    const double* charge;
+    const double* dipole;
+    const double* quadrupole;
+    double inertia[3];
+} md_component;
+
+typedef struct {
+    int64_t n_inner;        /* molecules in the box                                      */
+    int64_t n_halo;         /* periodic halo copies built                                */
+    int64_t max_occupancy;  /* largest number of molecules in one cell                   */
+    int64_t n_wrapped;      /* molecules moved back into the box this call               */
+    int32_t cells[3];       /* cells per dimension including the halo layer              */
+    int32_t reserved;
+    double cell_length[3];
+} md_bin_stats;
+
+typedef struct {
+    double upot;            /* Domain local Upot  = upot6lj/6 + upot_xpoles + my_rf      */
+    double virial;          /* Domain local virial = virial_pairs + 3 my_rf              */
+    double my_rf;           /* reaction-field term (-sum rffac e1.e2)                     */
+    double upot6lj;
+    double upot_xpoles;
+    double virial_pairs;
+    int64_t mol_pairs;      /* unique molecule pairs with centre distance^2 < rc^2       */
+    int64_t site_pairs[MD_NUM_KINDS]; /* unique interacting site pairs per kind          */
+} md_forces_out;
+
+typedef struct {
+    double summv2;          /* sum m v^2 over inner molecules                             */
+    double sumIw2;          /* sum I w^2                                                 */
+    int64_t n;
+    int64_t rot_dof;
+} md_kinetic_out;
+
+typedef struct {
+    double upot, virial, summv2, sumIw2;
+} md_step_record;
+
+int md_create(md_ctx** ctx, const md_config* cfg);
+int md_destroy(md_ctx* ctx);
+const char* md_last_error(const md_ctx* ctx);
+
+/* mixing: ncomp*(ncomp-1)/2 rows of (xi, eta) for the pairs (i<j) in row order. */
+int md_set_components(md_ctx* ctx, const md_component* comps, int32_t ncomp, const double* mixing);
+
+/* r, v, L: n x 3; q: n x 4 (w, x, y, z); comp: 0-based component index. */
+int md_upload_molecules(md_ctx* ctx, int64_t n, const uint64_t* id, const int32_t* comp,
+                        const double* r, const double* v, const double* q, const double* L);
+
+/* Outputs in upload order; any pointer may be NULL.  F, M, Vi are those of the
+ * last force evaluation. */
+int md_download_molecules(md_ctx* ctx, int64_t n, uint64_t* id, int32_t* comp, double* r, double* v,
+                          double* q, double* L, double* F, double* M, double* Vi);
+
+int md_rebin_and_halo(md_ctx* ctx, md_bin_stats* stats);
+int md_get_cell_assignment(md_ctx* ctx, int64_t n, int64_t* cell);
+int md_compute_forces(md_ctx* ctx, md_forces_out* out);
+int md_integrate_pre(md_ctx* ctx, double dt);
+int md_integrate_post(md_ctx* ctx, double dt, md_kinetic_out* out);
+
+/* nsteps full NVE steps on the device (pre-force half step, rebin + halo,
+ * forces, post-force half step, sums) with no host synchronisation between
+ * steps; rec (nsteps entries, may be NULL) receives the per-step sums. */
+int md_run(md_ctx* ctx, double dt, int32_t nsteps, md_step_record* rec);
+
+/* Wait for all work of the context. */
+int md_sync(md_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LS1GB300_H */

@@ -1,0 +1,124 @@
+"""ctypes binding of the C oracle (test infrastructure only).
+
+Used as the checker by tests/, by ``__graft_entry__.smoke()`` and by the CPU
+baseline of ``bench.py``; the engine never imports it.  ``build()`` compiles
+``liboracle.so`` with the Makefile beside this file.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+if os.path.join(ROOT, "ls1-mardyn_gb300") not in sys.path:
+    sys.path.insert(0, os.path.join(ROOT, "ls1-mardyn_gb300"))
+from ls1gb300 import abi  # noqa: E402
+
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(
+            os.path.join(HERE, "md_oracle.c")):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        vp, i64, i32, dp = C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double)
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [C.POINTER(abi.MdConfig), C.POINTER(abi.MdComponent), i32, dp]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_set_threads.argtypes = [i32]
+        L.orc_set_molecules.argtypes = [vp, i64, C.c_void_p, C.c_void_p, dp, dp, dp, dp]
+        L.orc_num_molecules.restype = i64
+        L.orc_num_molecules.argtypes = [vp]
+        L.orc_get_molecules.argtypes = [vp, i64] + [C.c_void_p] * 9
+        L.orc_rebin_and_halo.argtypes = [vp, C.POINTER(abi.MdBinStats)]
+        L.orc_get_cells.argtypes = [vp, i64, C.c_void_p]
+        L.orc_forces.argtypes = [vp, C.POINTER(abi.MdForcesOut), dp]
+        L.orc_pre.argtypes = [vp, C.c_double]
+        L.orc_post.argtypes = [vp, C.c_double, C.POINTER(abi.MdKineticOut)]
+        L.orc_run.argtypes = [vp, C.c_double, i32, C.POINTER(abi.MdStepRecord)]
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    """One box held by the CPU oracle (same call sequence as the engine)."""
+
+    def __init__(self, ps, rc, rc_lj=None, periodic=(1, 1, 1), threads: int = 1):
+        L = lib()
+        self.ps = ps
+        self.cfg = abi.make_config(ps.box, rc, rc if rc_lj is None else rc_lj, ps.eps_rf, periodic)
+        self.tables = abi.ComponentTables(ps.components, ps.mixing)
+        L.orc_set_threads(threads)
+        self.h = L.orc_create(C.byref(self.cfg), self.tables.array, self.tables.ncomp, self.tables.mixing)
+        if not self.h:
+            raise RuntimeError("orc_create failed")
+        ids, comp, r, v, q, Lm = abi.molecule_arrays(ps)
+        rc_ = L.orc_set_molecules(self.h, ps.n, ids.ctypes.data, comp.ctypes.data, abi.dptr(r), abi.dptr(v),
+                                  abi.dptr(q), abi.dptr(Lm))
+        if rc_:
+            raise RuntimeError(f"orc_set_molecules: {rc_}")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    @property
+    def n(self) -> int:
+        return int(lib().orc_num_molecules(self.h))
+
+    def rebin(self):
+        st = abi.MdBinStats()
+        rc = lib().orc_rebin_and_halo(self.h, C.byref(st))
+        if rc:
+            raise RuntimeError(f"orc_rebin_and_halo: {rc}")
+        return st
+
+    def cells(self) -> np.ndarray:
+        out = np.zeros(self.n, np.int64)
+        lib().orc_get_cells(self.h, self.n, out.ctypes.data)
+        return out
+
+    def forces(self):
+        fo = abi.MdForcesOut()
+        kc = np.zeros(8)
+        lib().orc_forces(self.h, C.byref(fo), abi.dptr(kc))
+        return fo, kc
+
+    def pre(self, dt):
+        lib().orc_pre(self.h, dt)
+
+    def post(self, dt):
+        ko = abi.MdKineticOut()
+        lib().orc_post(self.h, dt, C.byref(ko))
+        return ko
+
+    def run(self, dt, nsteps):
+        rec = (abi.MdStepRecord * max(nsteps, 1))()
+        rc = lib().orc_run(self.h, dt, nsteps, rec)
+        if rc:
+            raise RuntimeError(f"orc_run: {rc}")
+        return np.array([[x.upot, x.virial, x.summv2, x.sumIw2] for x in rec[:nsteps]])
+
+    def molecules(self):
+        n = self.n
+        out = dict(ids=np.zeros(n, np.uint64), comp=np.zeros(n, np.int32), r=np.zeros((n, 3)), v=np.zeros((n, 3)),
+                   q=np.zeros((n, 4)), L=np.zeros((n, 3)), F=np.zeros((n, 3)), M=np.zeros((n, 3)),
+                   Vi=np.zeros((n, 3)))
+        lib().orc_get_molecules(self.h, n, *(out[k].ctypes.data for k in
+                                             ("ids", "comp", "r", "v", "q", "L", "F", "M", "Vi")))
+        return out
