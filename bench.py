@@ -1,0 +1,335 @@
+"""Benchmark: molecule-updates/s of the short-range MD step on one GB300.
+
+Workload (default, the precision-form 1CLJ case at scale): single-centre LJ
+(eps = sigma = m = 1), fcc 100^3 x 4 = 4,000,000 molecules at rho* = 0.75,
+Maxwell-Boltzmann velocities at T* = 0.9 (seeded, net momentum removed),
+rc = 3.0 sigma, dt = 0.002, periodic box, NVE Leapfrog, mixed precision (FP32
+pair arithmetic, compensated per-molecule sums, FP64 state).  A "step" is one
+full MD step: pre-force half step, rebin/halo + pair-candidate list when due,
+forces, post-force half step and the Upot/virial/kinetic sums.
+
+  value   molecule-updates/s with the state resident in HBM, device-timed with
+          CUDA events on the engine's stream (max over ranks);
+  e2e     the same metric through the C ABI from host buffers: upload of the
+          phase space, the K steps with the per-step sums read back, and the
+          download of the final phase space, all inside the timed region;
+  roofline  the pair kernel (dominant kernel) against the FP32 FMA rate;
+  cpu_baseline  the CPU oracle (C restatement of the reference's path, OpenMP
+          C08 traversal) on all host cores on a bounded sample of the workload.
+
+--impl reference times that CPU path alone (rank 0; other ranks exit 0).
+Multi-GPU: independent replicas (one box per rank, no collective on the data
+path), value = all ranks' updates / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "ls1-mardyn_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+from ls1gb300 import phasespace as psm  # noqa: E402
+
+WORKLOADS = {
+    # name: (generator, rc, dt, description)
+    "lj4m": (lambda: psm.lj_fcc(100, 0.75, 0.9, seed=2024), 3.0, 0.002,
+             "1CLJ fcc 100^3x4 = 4,000,000, rho*=0.75, T*=0.9, rc=3.0, dt=0.002"),
+    "lj32k": (lambda: psm.lj_fcc(20, 0.8, 1.0, seed=1), 2.5, 0.002,
+              "1CLJ fcc 20^3x4 = 32,000, rho*=0.8, T*=1.0, rc=2.5, dt=0.002"),
+    "slab": (lambda: psm.lj_slab(91, 0.73, 0.02, 0.9, seed=2025), 3.0, 0.002,
+             "1CLJ vapour-liquid slab, 3.2M molecules, rho_l*=0.73, rho_v*=0.02, T*=0.9, rc=3.0"),
+    "mix1m": (lambda: psm.mixture(1_000_000, 18.0, 300.0, seed=2026), 1.0, 9.118e-5,
+              "2CLJQ/1CLJD 50/50 mixture, N=1,000,188, n=18 nm^-3, T=300 K, rc=1 nm, RF eps=1e10, dt=1 fs"),
+}
+DEFAULT_SKIN = {"lj4m": 0.3, "lj32k": 0.3, "slab": 0.3, "mix1m": 0.1}
+FLOP_PER_PAIR_LJ = 39.0  # reference FlopCounter model: 31 per LJ site pair + 8 per molecule distance
+
+
+# ---------------------------------------------------------------- CUDA events on the engine stream
+class Cudart:
+    def __init__(self):
+        import glob
+        cands = sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*")) + ["libcudart.so"]
+        self.L = None
+        for c in cands:
+            try:
+                self.L = C.CDLL(c)
+                break
+            except OSError:
+                continue
+        if self.L is None:
+            raise RuntimeError("libcudart not found")
+        self.L.cudaEventCreate.argtypes = [C.POINTER(C.c_void_p)]
+        self.L.cudaEventRecord.argtypes = [C.c_void_p, C.c_void_p]
+        self.L.cudaEventSynchronize.argtypes = [C.c_void_p]
+        self.L.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
+        self.L.cudaEventDestroy.argtypes = [C.c_void_p]
+
+    def event(self):
+        e = C.c_void_p()
+        assert self.L.cudaEventCreate(C.byref(e)) == 0
+        return e
+
+    def record(self, e, stream):
+        assert self.L.cudaEventRecord(e, C.c_void_p(stream)) == 0
+
+    def elapsed_ms(self, a, b) -> float:
+        assert self.L.cudaEventSynchronize(b) == 0
+        ms = C.c_float()
+        assert self.L.cudaEventElapsedTime(C.byref(ms), a, b) == 0
+        return float(ms.value)
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU baseline (oracle)
+def cpu_baseline(workload: str, budget_s: float = 12.0) -> dict:
+    from oracle.oracle import Oracle
+    gen, rc, dt, _ = WORKLOADS[workload]
+    if workload in ("lj4m", "slab"):
+        ps = psm.lj_fcc(14, 0.75, 0.9, seed=7)        # 10,976 molecules, same state point
+        sample = "1CLJ fcc 14^3x4 = 10,976 molecules at the same rho*, T*, rc, dt"
+    elif workload == "lj32k":
+        ps = gen()
+        sample = "the full 32,000-molecule box"
+    else:
+        ps = psm.mixture(4000, 18.0, 300.0, seed=7)
+        sample = "2CLJQ/1CLJD mixture, 4,000 molecules, same state point"
+    threads = os.cpu_count() or 1
+    o = Oracle(ps, rc, threads=threads)
+    o.rebin()
+    o.forces()
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        o.run(dt, 5)
+        steps += 5
+        el = time.perf_counter() - t0
+        if el > budget_s:
+            break
+    return {"value": ps.n * steps / el, "unit": "molecule-updates/s", "cores": threads, "kind": "port",
+            "sample": f"{sample}; {steps} NVE steps in {el:.1f} s with {threads} OpenMP threads"}
+
+
+# ---------------------------------------------------------------- main
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="lj4m", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--skin", type=float, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(a, rank):
+    if rank != 0:
+        return
+    cb = cpu_baseline(a.workload, budget_s=max(10.0, min(60.0, 0.5 * a.steps)))
+    gen, rc, dt, desc = WORKLOADS[a.workload]
+    line = {"impl": "reference", "metric": "molecule-updates/s", "value": cb["value"], "unit": "molecule-updates/s",
+            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": {"workload": desc, "sample": cb["sample"]},
+            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "molecule-updates/s",
+                                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    a = parse()
+    rank, world, local, pg = dist_setup()
+    if a.impl == "reference":
+        run_reference(a, rank)
+        return
+    import build as engine_build
+    if rank == 0:
+        engine_build.build()
+    barrier(pg)
+    from ls1gb300 import engine as E
+
+    gen, rc, dt, desc = WORKLOADS[a.workload]
+    skin = DEFAULT_SKIN[a.workload] if a.skin is None else a.skin
+    ps = gen()
+    n = ps.n
+    cu = Cudart()
+
+    # ---- device-resident timing
+    eng = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local)
+    fo0 = eng.forces()
+    eng.run(dt, max(3, a.warmup), record=False)
+    eng.sync()
+    stream = eng.stream()
+    t_clock = ClockSampler(local)
+    barrier(pg)
+    e0, e1 = cu.event(), cu.event()
+    t_clock.start()
+    cu.record(e0, stream)
+    eng.run(dt, a.steps, record=True)
+    cu.record(e1, stream)
+    ms = cu.elapsed_ms(e0, e1)
+    clocks = t_clock.stop()
+    ms = max_over_ranks(pg, ms)
+    value = world * n * a.steps / (ms * 1e-3)
+    # per-kernel times on the engine stream, right after the timed region
+    fo = eng.forces()
+    kt = eng.time_kernels(5)
+    pairs = fo.site_pairs[0]
+    flops = FLOP_PER_PAIR_LJ * pairs
+    fp32_peak = 152 * 128 * 2 * 2070e6 / 1e12   # TFLOP/s at the maximum SM clock
+    achieved = flops / (kt.force_ms * 1e-3) / 1e12
+    list_bytes = kt.mean_candidates * n * 4.0
+    hbm_bytes = list_bytes + n * (16 + 4 + 9 * 8)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm_peak, hbm_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        hbm_peak, hbm_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    eng.close()
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not a.no_e2e:
+        ids, comp, r, v, q, Lm = E.abi.molecule_arrays(ps)
+        t0 = time.perf_counter()
+        eng2 = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local)
+        eng2.forces()
+        rec = eng2.run(dt, a.steps, record=True)
+        out = eng2.molecules()
+        t1 = time.perf_counter()
+        e2e_s = max_over_ranks(pg, t1 - t0)
+        eng2.close()
+        h2d = sum(x.nbytes for x in (ids, comp, r, v, q, Lm))
+        d2h = sum(out[k].nbytes for k in out) + rec.nbytes
+        e2e = {"value": world * n * a.steps / e2e_s, "unit": "molecule-updates/s",
+               "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps,
+               "scope": "md_create + upload + first forces + K steps (per-step sums read back) + download"}
+
+    cb = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        cb = cpu_baseline(a.workload)
+
+    if rank == 0:
+        line = {
+            "metric": "molecule-updates/s", "value": value, "unit": "molecule-updates/s", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32-pairs/f64-state" if a.precision == "mixed" else "f64",
+            "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann velocities)",
+            "config": {"workload": desc, "precision": a.precision, "skin": skin, "molecules": n,
+                       "parallelism": f"replicas x{world}", "l2": "working set > L2 (GBs), no flush needed"},
+            "gpu_launches": int(kt.launches_per_step * a.steps),
+            "roofline": {"bound": "fp32", "kernel": "k_force_lj<float>", "achieved": achieved, "peak": fp32_peak,
+                         "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                         "algorithmic": f"{FLOP_PER_PAIR_LJ:.0f} flop x {pairs} unique in-cutoff pairs per launch",
+                         "launch_ms": kt.force_ms,
+                         "peak_source": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 flop x 2070 MHz"},
+            "roofline_hbm": {"bound": "hbm", "achieved": hbm_bytes / (kt.force_ms * 1e-3) / 1e9, "peak": hbm_peak,
+                             "unit": "GB/s", "frac": hbm_bytes / (kt.force_ms * 1e-3) / 1e9 / hbm_peak,
+                             "peak_source": hbm_src,
+                             "algorithmic": "pair-candidate list (4 B/entry) + positions + outputs per launch"},
+            "kernels_ms": {"force": kt.force_ms, "pre": kt.pre_ms, "post": kt.post_ms, "rebuild": kt.rebuild_ms},
+            "pair_list": {"mean_candidates": kt.mean_candidates, "rebuilds": int(kt.rebuilds)},
+            "physics": {"upot_per_molecule": fo.upot / n, "unique_lj_pairs": int(pairs)},
+            "clocks": clocks,
+            "e2e": e2e,
+            "cpu_baseline": cb,
+        }
+        print(json.dumps(line))
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -154,6 +154,26 @@ int md_run(md_ctx* ctx, double dt, int32_t nsteps, md_step_record* rec);
 /* Wait for all work of the context. */
 int md_sync(md_ctx* ctx);
 
+/* ---- measurement hooks (no counterpart in the reference; used by bench.py)
+ * md_get_stream: the CUDA stream (cudaStream_t) every kernel of the context
+ * runs on, so a caller can bracket calls with its own CUDA events.
+ * md_time_kernels: mean device time of each kernel family, measured with
+ * CUDA events on that stream over `reps` back-to-back launches on the current
+ * state (the pair-candidate list is left as it is). */
+typedef struct {
+    double force_ms;          /* one pair-kernel launch (k_force_*)                     */
+    double pre_ms;            /* one pre-force Leapfrog half step                       */
+    double post_ms;           /* one post-force half step + sums                        */
+    double rebuild_ms;        /* one forced rebin + list rebuild                        */
+    double mean_candidates;   /* mean pair-candidate list length per molecule           */
+    int64_t rebuilds;         /* list rebuilds since md_create                          */
+    int32_t launches_per_step;/* kernels one md_run step launches                       */
+    int32_t reserved;
+} md_kernel_times;
+
+int md_get_stream(md_ctx* ctx, void** stream);
+int md_time_kernels(md_ctx* ctx, int32_t reps, md_kernel_times* out);
+
 #ifdef __cplusplus
 }
 #endif

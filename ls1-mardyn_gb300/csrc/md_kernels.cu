@@ -1,0 +1,778 @@
+// md_kernels.cu -- all device kernels of the engine and the C-ABI host code.
+//
+// Kernel map (reference function each one replaces, paths relative to the
+// ls1-mardyn tree):
+//   k_wrap              DomainDecompBase::handleDomainLeavingParticles (DomainDecompBase.cpp:199-249)
+//   k_ref_cells         LinkedCells::getCellIndexOfPoint (LinkedCells.cpp:870-923)
+//   k_halo_count        DomainDecompBase::populateHaloLayerWithCopies (DomainDecompBase.cpp:317-376):
+//                       number of halo copies each molecule generates
+//   k_list_hist/scan/   LinkedCells::update + FullParticleCell::buildSoACaches: counting sort
+//   k_list_scatter/     of the molecules into cells, slots re-sorted into cell order
+//   k_cell_sort/k_permute
+//   k_build_list        C08CellPairTraversal over the 27-cell neighbourhood (C08CellPairTraversal.h,
+//                       C08BasedTraversals.h:48-152) -> owner-computes pair-candidate list
+//   k_sites             FullMolecule::setupSoACache (FullMolecule.cpp:711-767)
+//   k_force_lj / k_force_ms
+//                       VectorizedCellProcessor::_calculatePairs + _loopBody* (VCP.cpp:171-2730)
+//                       fused with FullMolecule::calcFM (FullMolecule.cpp:548-631)
+//   k_pre               FullMolecule::upd_preF (FullMolecule.cpp:331-361)
+//   k_post              FullMolecule::upd_postF + Leapfrog::transition2to3 (Leapfrog.cpp:63-147)
+//   k_finalize          VCP::endTraversal (VCP.cpp:122-155), Domain local sums
+#include "md_device.cuh"
+#include "md_pair.cuh"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "../../include/ls1gb300.h"
+
+using namespace md;
+
+__constant__ Params cP;
+
+// status word bits (device -> host)
+#define ST_LOST 1u
+#define ST_LIST_OVERFLOW 2u
+#define ST_NAN 4u
+#define ST_CELL_SORT 8u
+
+struct Scratch {
+    // reductions
+    double* partials;       // [nblocks_max * NPART]
+    double* result;         // finalize output (NPART doubles)
+    md_step_record* records;
+    int* step;              // step counter for md_run records
+    unsigned* status;
+    unsigned* need_rebuild;
+    unsigned* disp_max;     // float bits
+    int* list_need;         // max candidates needed (overflow report)
+};
+
+#define NPART 16   // partial-sum slots per block
+// slots: 0 upot6lj 1 upotXpoles 2 virial 3 myRF 4 mol_pairs 5..11 site pairs 12 summv2 13 sumIw2 14 n 15 rotdof
+
+// ------------------------------------------------------------------ reductions
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum `v` over the block (blockDim multiple of 32, <= 1024); result valid in thread 0.
+__device__ double block_sum(double v, double* sh) {
+    v = warp_sum(v);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x < 32) {
+        int nw = blockDim.x >> 5;
+        r = threadIdx.x < nw ? sh[threadIdx.x] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+__global__ void k_zero_partials(double* partials, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) partials[i] = 0.0;
+}
+
+// Fixed-order sum of the per-block partials (deterministic), one block.
+__global__ void k_finalize(const double* partials, int nblocks, double* result, md_step_record* rec, int* step,
+                           int record) {
+    __shared__ double sh[32];
+    for (int s = 0; s < NPART; ++s) {
+        double v = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v += partials[(size_t)b * NPART + s];
+        v = block_sum(v, sh);
+        if (threadIdx.x == 0) result[s] = v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && record) {
+        int k = *step;
+        double myRF = result[3];
+        rec[k].upot = result[0] / 6.0 + result[1] + myRF;
+        rec[k].virial = result[2] + 3.0 * myRF;
+        rec[k].summv2 = result[12];
+        rec[k].sumIw2 = result[15] > 0.0 ? result[13] : 0.0;
+        *step = k + 1;
+    }
+}
+
+// ------------------------------------------------------------------ wrap + cells
+__device__ __forceinline__ double& coord(State& S, int d, int64_t i) {
+    return d == 0 ? S.rx[i] : d == 1 ? S.ry[i] : S.rz[i];
+}
+
+// DomainDecompBase::handleDomainLeavingParticles for every periodic dimension:
+// lower face first (shift +L, clamp below max), then upper face (shift -L,
+// clamp to min).  Molecules further than rc outside the box are lost in the
+// reference; they raise ST_LOST here.
+__global__ void k_wrap(State S, unsigned* status, unsigned long long* nwrapped, const unsigned* need) {
+    if (need && !*need) return;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    double r[3] = {S.rx[i], S.ry[i], S.rz[i]};
+    int moved = 0;
+    for (int d = 0; d < 3; ++d) {
+        if (!cP.periodic[d]) continue;
+        double lo[3], hi[3];
+        for (int e = 0; e < 3; ++e) { lo[e] = cP.bmin[e] - cP.rc; hi[e] = cP.bmax[e] + cP.rc; }
+        // direction -: region [min - rc, min) in d
+        bool inreg = true;
+        for (int e = 0; e < 3; ++e) {
+            double l = lo[e], h = (e == d) ? cP.bmin[d] : hi[e];
+            inreg &= (r[e] >= l && r[e] < h);
+        }
+        if (inreg) {
+            r[d] = r[d] + cP.L[d];
+            if (r[d] >= cP.bmax[d]) r[d] = next_down(cP.bmax[d]);
+            moved = 1;
+        }
+        inreg = true;
+        for (int e = 0; e < 3; ++e) {
+            double l = (e == d) ? cP.bmax[d] : lo[e], h = hi[e];
+            inreg &= (r[e] >= l && r[e] < h);
+        }
+        if (inreg) {
+            r[d] = r[d] + (-cP.L[d]);
+            if (r[d] <= cP.bmin[d]) r[d] = cP.bmin[d];
+            moved = 1;
+        }
+    }
+    for (int d = 0; d < 3; ++d)
+        if (cP.periodic[d] && !(r[d] >= cP.bmin[d] && r[d] < cP.bmax[d])) atomicOr(status, ST_LOST);
+    if (moved) {
+        S.rx[i] = r[0]; S.ry[i] = r[1]; S.rz[i] = r[2];
+        atomicAdd(nwrapped, 1ull);
+    }
+}
+
+// LinkedCells::getCellIndexOfPoint with the border table of
+// CellBorderAndFlagManager::getBorder (arithmetic kept unfused).
+__device__ int64_t ref_cell_of_point(const double* point, const double* border, int bstride) {
+    int ci[3];
+    double p[3] = {point[0], point[1], point[2]};
+    for (int d = 0; d < 3; ++d) {
+        if (p[d] <= cP.rhmin[d]) p[d] = __dadd_rn(p[d], __dmul_rn(cP.rcl[d], 0.5));
+        else if (p[d] >= cP.rhmax[d]) p[d] = __dsub_rn(p[d], __dmul_rn(cP.rcl[d], 0.5));
+        int c = (int)floor(__dmul_rn(__dsub_rn(p[d], cP.bmin[d]), cP.rclr[d])) + 1;
+        c = max(0, min(c, cP.rcpd[d] - 1));
+        ci[d] = c;
+    }
+    bool inside = true;
+    for (int d = 0; d < 3; ++d)
+        inside &= (border[d * bstride + ci[d]] <= p[d]) && (p[d] < border[d * bstride + ci[d] + 1]);
+    if (!inside) {
+        for (int d = 0; d < 3; ++d) {
+            if (p[d] < border[d * bstride + ci[d]]) ci[d]--;
+            else if (p[d] >= border[d * bstride + ci[d] + 1]) ci[d]++;
+        }
+    }
+    return ((int64_t)ci[2] * cP.rcpd[1] + ci[1]) * cP.rcpd[0] + ci[0];
+}
+
+__global__ void k_ref_cells(State S, const double* border, int bstride, int64_t* cell_out_upload_order,
+                            unsigned* occupancy) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    double p[3] = {S.rx[i], S.ry[i], S.rz[i]};
+    int64_t c = ref_cell_of_point(p, border, bstride);
+    if (cell_out_upload_order) cell_out_upload_order[S.orig[i]] = c;
+    if (occupancy) atomicAdd(&occupancy[c], 1u);
+}
+
+// Halo copies of DomainDecompBase::populateHaloLayerWithCopies: a molecule in
+// [min, min+rc) or [max-rc, max) of a periodic dimension is copied there, and
+// copies of earlier dimensions are copied again, so it generates
+// prod_d (1 + near_d) - 1 copies; each copy is binned into its halo cell.
+__global__ void k_halo(State S, const double* border, int bstride, unsigned long long* nhalo, unsigned* occupancy) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    double r[3] = {S.rx[i], S.ry[i], S.rz[i]};
+    int sh[3];
+    int cnt = 1;
+    for (int d = 0; d < 3; ++d) {
+        sh[d] = 0;
+        if (!cP.periodic[d]) continue;
+        if (r[d] >= cP.bmin[d] && r[d] < cP.bmin[d] + cP.rc) sh[d] = 1;
+        else if (r[d] >= cP.bmax[d] - cP.rc && r[d] < cP.bmax[d]) sh[d] = -1;
+        if (sh[d]) cnt *= 2;
+    }
+    if (cnt == 1) return;
+    atomicAdd(nhalo, (unsigned long long)(cnt - 1));
+    if (!occupancy) return;
+    for (int m = 1; m < 8; ++m) {
+        bool ok = true;
+        double p[3];
+        for (int d = 0; d < 3; ++d) {
+            int use = (m >> d) & 1;
+            if (use && !sh[d]) { ok = false; break; }
+            p[d] = r[d];
+            if (use) {
+                if (sh[d] > 0) { p[d] = r[d] + cP.L[d]; if (p[d] < cP.bmax[d]) p[d] = next_up(cP.bmax[d]); }
+                else { p[d] = r[d] + (-cP.L[d]); if (p[d] >= cP.bmin[d]) p[d] = next_down(cP.bmin[d]); }
+            }
+        }
+        if (!ok) continue;
+        atomicAdd(&occupancy[ref_cell_of_point(p, border, bstride)], 1u);
+    }
+}
+
+__global__ void k_max_u32(const unsigned* a, int64_t n, unsigned* out) {
+    unsigned m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, a[i]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// ------------------------------------------------------------------ list-grid binning
+__device__ __forceinline__ int list_cell_coord(double x, int d) {
+    int c = (int)floor((x - cP.bmin[d]) * cP.linv[d]);
+    return max(0, min(c, cP.ln[d] - 1));
+}
+
+__global__ void k_list_hist(State S, int* mcell, int* counts, const unsigned* need) {
+    if (!*need) return;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    int cx = list_cell_coord(S.rx[i], 0), cy = list_cell_coord(S.ry[i], 1), cz = list_cell_coord(S.rz[i], 2);
+    int c = (cz * cP.ln[1] + cy) * cP.ln[0] + cx;
+    mcell[i] = c;
+    atomicAdd(&counts[c], 1);
+}
+
+// Exclusive scan of counts[0..n) into start[0..n], one block of 1024 threads.
+__global__ void k_scan(const int* counts, int* start, int n, int* cursor, const unsigned* need) {
+    if (!*need) return;
+    __shared__ int sh[1024];
+    int per = (n + blockDim.x - 1) / blockDim.x;
+    int b = threadIdx.x * per, e = min(n, b + per);
+    int s = 0;
+    for (int k = b; k < e; ++k) s += counts[k];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < blockDim.x; off <<= 1) {
+        int v = threadIdx.x >= off ? sh[threadIdx.x - off] : 0;
+        __syncthreads();
+        sh[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int run = sh[threadIdx.x] - s;
+    for (int k = b; k < e; ++k) {
+        start[k] = run;
+        cursor[k] = run;
+        run += counts[k];
+    }
+    if (threadIdx.x == blockDim.x - 1) start[n] = sh[threadIdx.x];
+}
+
+__global__ void k_list_scatter(int64_t n, const int* mcell, int* cursor, int* perm, const unsigned* need) {
+    if (!*need) return;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int p = atomicAdd(&cursor[mcell[i]], 1);
+    perm[p] = (int)i;
+}
+
+// Deterministic order inside each cell: sort the slot indices of the cell.
+__global__ void k_cell_sort(const int* start, int ncells, int* perm, const unsigned* need) {
+    if (!*need) return;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    int b = start[c], e = start[c + 1];
+    for (int k = b + 1; k < e; ++k) {
+        int v = perm[k];
+        int m = k - 1;
+        while (m >= b && perm[m] > v) { perm[m + 1] = perm[m]; --m; }
+        perm[m + 1] = v;
+    }
+}
+
+// Gather all master arrays into slot order (dst = src[perm]).
+__global__ void k_permute(State dst, State src, const int* perm, const int* mcell, const unsigned* need) {
+    if (!*need) return;
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= src.n) return;
+    int64_t i = perm[k];
+#define PM(a) dst.a[k] = src.a[i]
+    PM(rx); PM(ry); PM(rz); PM(vx); PM(vy); PM(vz); PM(qw); PM(qx); PM(qy); PM(qz); PM(Lx); PM(Ly); PM(Lz);
+    PM(Fx); PM(Fy); PM(Fz); PM(Mx); PM(My); PM(Mz); PM(Vx); PM(Vy); PM(Vz); PM(comp); PM(orig); PM(id);
+#undef PM
+    dst.home[k] = mcell[i];
+}
+
+// Local coordinates relative to the home-cell origin (and a copy of the
+// reference positions for the displacement test).
+template <typename Real4>
+__device__ __forceinline__ void make_local(const State& S, int64_t i, Real4* xl) {
+    int h = S.home[i];
+    int cx = h % cP.ln[0], cy = (h / cP.ln[0]) % cP.ln[1], cz = h / (cP.ln[0] * cP.ln[1]);
+    double ox = cP.bmin[0] + cx * cP.lside[0], oy = cP.bmin[1] + cy * cP.lside[1], oz = cP.bmin[2] + cz * cP.lside[2];
+    Real4 p;
+    p.x = S.rx[i] - ox;
+    p.y = S.ry[i] - oy;
+    p.z = S.rz[i] - oz;
+    p.w = __int_as_float(S.comp[i]);
+    xl[i] = p;
+}
+
+__global__ void k_local(State S, float4* xlf, double* rref, const unsigned* need) {
+    if (need && !*need) return;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    make_local<float4>(S, i, xlf);
+    rref[3 * i] = S.rx[i]; rref[3 * i + 1] = S.ry[i]; rref[3 * i + 2] = S.rz[i];
+}
+
+// Owner-computes pair-candidate list over the 27 list cells around the home
+// cell (periodic wrap in periodic dimensions).  Candidate test in FP32 local
+// coordinates against (rc + skin)^2 enlarged by a relative 1e-4, so no pair
+// that can come within rc before the next rebuild is missed.
+__global__ void k_build_list(State S, const float4* xl, const int* start, uint32_t* nbr, int* nnb, int maxnb,
+                             int64_t cap, float rl2, unsigned* status, int* need_max, const unsigned* need) {
+    if (!*need) return;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    float4 pi = xl[i];
+    int h = S.home[i];
+    int hc[3] = {h % cP.ln[0], (h / cP.ln[0]) % cP.ln[1], h / (cP.ln[0] * cP.ln[1])};
+    float side[3] = {(float)cP.lside[0], (float)cP.lside[1], (float)cP.lside[2]};
+    int cnt = 0;
+    for (int oz = -1; oz <= 1; ++oz)
+        for (int oy = -1; oy <= 1; ++oy)
+            for (int ox = -1; ox <= 1; ++ox) {
+                int o[3] = {ox, oy, oz};
+                int c[3];
+                bool skip = false;
+                for (int d = 0; d < 3; ++d) {
+                    c[d] = hc[d] + o[d];
+                    if (c[d] < 0 || c[d] >= cP.ln[d]) {
+                        if (!cP.periodic[d]) { skip = true; break; }
+                        c[d] = (c[d] + cP.ln[d]) % cP.ln[d];
+                    }
+                }
+                if (skip) continue;
+                // with two cells along a periodic axis both offsets reach the same
+                // cell; the far image is removed by the distance test
+                int cell = (c[2] * cP.ln[1] + c[1]) * cP.ln[0] + c[0];
+                uint32_t code = (uint32_t)((ox + 1) + 3 * (oy + 1) + 9 * (oz + 1));
+                float offx = ox * side[0], offy = oy * side[1], offz = oz * side[2];
+                for (int j = start[cell]; j < start[cell + 1]; ++j) {
+                    if (j == i) continue;
+                    float4 pj = xl[j];
+                    float dx = (pi.x - pj.x) - offx, dy = (pi.y - pj.y) - offy, dz = (pi.z - pj.z) - offz;
+                    float r2 = dx * dx + dy * dy + dz * dz;
+                    if (r2 < rl2) {
+                        if (cnt < maxnb) nbr[(int64_t)cnt * cap + i] = (uint32_t)j | (code << MD_CODE_SHIFT);
+                        ++cnt;
+                    }
+                }
+            }
+    nnb[i] = min(cnt, maxnb);
+    if (cnt > maxnb) {
+        atomicOr(status, ST_LIST_OVERFLOW);
+        atomicMax(need_max, cnt);
+    }
+}
+
+// ------------------------------------------------------------------ site cache
+// FullMolecule::setupSoACache: normalise q, rotate site offsets and
+// orientations.  Offsets are stored relative to the molecule centre.
+template <typename Real>
+__global__ void k_sites(State S, Real* sd, Real* se, int stride) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const CompDev& C = cP.comp[S.comp[i]];
+    double w = S.qw[i], x = S.qx[i], y = S.qy[i], z = S.qz[i];
+    double s = 1. / sqrt(w * w + x * x + y * y + z * z);
+    w *= s; x *= s; y *= s; z *= s;
+    S.qw[i] = w; S.qx[i] = x; S.qy[i] = y; S.qz[i] = z;
+    for (int k = 0; k < C.ns; ++k) {
+        double o[3];
+        qrot(w, x, y, z, C.d[k], o);
+        for (int e = 0; e < 3; ++e) sd[((int64_t)i * stride + k) * 3 + e] = (Real)o[e];
+        if (C.kind[k] >= SK_DIPOLE) {
+            qrot(w, x, y, z, C.e[k], o);
+            for (int e = 0; e < 3; ++e) se[((int64_t)i * stride + k) * 3 + e] = (Real)o[e];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ forces
+// FP64 image shift of neighbour j seen from i for cell-offset code `code`:
+// the reference's halo copy r_j +- L.
+__device__ __forceinline__ void image_shift(int h, uint32_t code, double* sh) {
+    int hc[3] = {h % cP.ln[0], (h / cP.ln[0]) % cP.ln[1], h / (cP.ln[0] * cP.ln[1])};
+    for (int d = 0; d < 3; ++d) {
+        int c = hc[d] + decode_o(code, d);
+        sh[d] = c < 0 ? -cP.L[d] : (c >= cP.ln[d] ? cP.L[d] : 0.0);
+    }
+}
+
+__device__ __forceinline__ double fp64_r2(const State& S, int64_t i, int64_t j, uint32_t code) {
+    double sh[3];
+    image_shift(S.home[i], code, sh);
+    double dx = S.rx[i] - (S.rx[j] + sh[0]);
+    double dy = S.ry[i] - (S.ry[j] + sh[1]);
+    double dz = S.rz[i] - (S.rz[j] + sh[2]);
+    return __dadd_rn(__dmul_rn(dx, dx), __dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dz, dz)));
+}
+
+template <typename Real> struct R4;
+template <> struct R4<float> { typedef float4 t; };
+template <> struct R4<double> { typedef double4 t; };
+
+// Single-LJ-centre molecules (centre at the molecule origin): the hot path
+// of the 1CLJ benchmarks.  One thread per molecule, list entries streamed
+// column-major.
+template <typename Real>
+__global__ void __launch_bounds__(256) k_force_lj(State S, const float4* xlf, const uint32_t* nbr, const int* nnb,
+                                                  int64_t cap, double* partials) {
+    __shared__ Real soff[27][3];
+    __shared__ double sh[32];
+    if (threadIdx.x < 27) {
+        int t = threadIdx.x;
+        soff[t][0] = (Real)((t % 3 - 1) * cP.lside[0]);
+        soff[t][1] = (Real)(((t / 3) % 3 - 1) * cP.lside[1]);
+        soff[t][2] = (Real)((t / 9 - 1) * cP.lside[2]);
+    }
+    __syncthreads();
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    typename Acc<Real>::type fx, fy, fz, vx, vy, vz, up, vir;
+    fx.init(); fy.init(); fz.init(); vx.init(); vy.init(); vz.init(); up.init(); vir.init();
+    double npairs = 0.0, nmol = 0.0;
+    if (i < S.n) {
+        const int ci = S.comp[i];
+        const int gi = cP.comp[ci].ljoff;
+        Real pix, piy, piz;
+        if (sizeof(Real) == 4) {
+            float4 p = xlf[i];
+            pix = p.x; piy = p.y; piz = p.z;
+        } else {
+            pix = S.rx[i]; piy = S.ry[i]; piz = S.rz[i];
+        }
+        const int cnt = nnb[i];
+        const Real rclj2 = sizeof(Real) == 4 ? (Real)cP.rclj2f : (Real)cP.rclj2;
+        const Real rc2 = sizeof(Real) == 4 ? (Real)cP.rc2f : (Real)cP.rc2;
+        Real e24 = (Real)cP.eps24[gi * cP.nlj + gi], s2 = (Real)cP.sig2[gi * cP.nlj + gi];
+        Real sh6 = (Real)cP.shift6[gi * cP.nlj + gi];
+        int cur = gi;
+        for (int k = 0; k < cnt; ++k) {
+            uint32_t e = __ldg(&nbr[(int64_t)k * cap + i]);
+            int64_t j = e & MD_INDEX_MASK;
+            uint32_t code = e >> MD_CODE_SHIFT;
+            Real dx, dy, dz;
+            if (sizeof(Real) == 4) {
+                float4 pj = __ldg(&xlf[j]);
+                dx = (pix - (Real)pj.x) - soff[code][0];
+                dy = (piy - (Real)pj.y) - soff[code][1];
+                dz = (piz - (Real)pj.z) - soff[code][2];
+            } else {
+                double shf[3];
+                image_shift(S.home[i], code, shf);
+                dx = pix - (S.rx[j] + shf[0]);
+                dy = piy - (S.ry[j] + shf[1]);
+                dz = piz - (S.rz[j] + shf[2]);
+            }
+            Real r2 = dx * dx + (dy * dy + dz * dz);
+            bool in = r2 < rclj2, in_rc = r2 < rc2;
+            if (sizeof(Real) == 4) {
+                bool bl = r2 > (Real)cP.band_lo_lj && r2 < (Real)cP.band_hi_lj;
+                bool be = r2 > (Real)cP.band_lo && r2 < (Real)cP.band_hi;
+                if (bl || be) {
+                    double r2d = fp64_r2(S, i, j, code);
+                    if (bl) in = r2d < cP.rclj2;
+                    if (be) in_rc = r2d < cP.rc2;
+                }
+            }
+            if (in_rc && j > i) nmol += 1.0;
+            if (!in) continue;
+            const int gj = cP.comp[S.comp[j]].ljoff;
+            if (gj != cur) {
+                cur = gj;
+                e24 = (Real)cP.eps24[gi * cP.nlj + gj];
+                s2 = (Real)cP.sig2[gi * cP.nlj + gj];
+                sh6 = (Real)cP.shift6[gi * cP.nlj + gj];
+            }
+            Real f[3], V[3], u;
+            const Real d[3] = {dx, dy, dz};
+            lj_pair<Real>(d, d, r2, e24, s2, sh6, f, V, u);
+            fx.add(f[0]); fy.add(f[1]); fz.add(f[2]);
+            vx.add(V[0]); vy.add(V[1]); vz.add(V[2]);
+            if (j > i) {
+                up.add(u);
+                vir.add(V[0] + V[1] + V[2]);
+                npairs += 1.0;
+            }
+        }
+        S.Fx[i] = fx.value(); S.Fy[i] = fy.value(); S.Fz[i] = fz.value();
+        S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
+        S.Vx[i] = 0.5 * vx.value(); S.Vy[i] = 0.5 * vy.value(); S.Vz[i] = 0.5 * vz.value();
+    }
+    double* P = partials + (size_t)blockIdx.x * NPART;
+    double t;
+    t = block_sum(up.value(), sh); if (threadIdx.x == 0) P[0] = t;
+    t = block_sum(vir.value(), sh); if (threadIdx.x == 0) P[2] = t;
+    t = block_sum(npairs, sh);
+    if (threadIdx.x == 0) { P[1] = 0.0; P[3] = 0.0; P[5] = t; for (int s = 6; s < 12; ++s) P[s] = 0.0; }
+    t = block_sum(nmol, sh);
+    if (threadIdx.x == 0) P[4] = t;
+}
+
+// General multi-site molecules: all site pairs of every molecule pair inside
+// the molecule-centre cut-off (rc_lj for LJ centres, rc for the multipoles),
+// with calcFM folded in: F = sum f, M = sum d_site x f + multipole torques,
+// Vi = 1/2 sum m_d o f.
+template <typename Real>
+__global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, const Real* sd, const Real* se,
+                                                  int stride, const uint32_t* nbr, const int* nnb, int64_t cap,
+                                                  double* partials) {
+    __shared__ Real soff[27][3];
+    __shared__ double sh[32];
+    if (threadIdx.x < 27) {
+        int t = threadIdx.x;
+        soff[t][0] = (Real)((t % 3 - 1) * cP.lside[0]);
+        soff[t][1] = (Real)(((t / 3) % 3 - 1) * cP.lside[1]);
+        soff[t][2] = (Real)((t / 9 - 1) * cP.lside[2]);
+    }
+    __syncthreads();
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    typename Acc<Real>::type F[3], M[3], V[3], u6, ux, vir, rf;
+    for (int e = 0; e < 3; ++e) { F[e].init(); M[e].init(); V[e].init(); }
+    u6.init(); ux.init(); vir.init(); rf.init();
+    double cnt_pairs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (i < S.n) {
+        const int ci = S.comp[i];
+        const CompDev& A = cP.comp[ci];
+        Real pi[3];
+        if (sizeof(Real) == 4) {
+            float4 p = xlf[i];
+            pi[0] = p.x; pi[1] = p.y; pi[2] = p.z;
+        } else {
+            pi[0] = S.rx[i]; pi[1] = S.ry[i]; pi[2] = S.rz[i];
+        }
+        const int cnt = nnb[i];
+        const Real rclj2 = sizeof(Real) == 4 ? (Real)cP.rclj2f : (Real)cP.rclj2;
+        const Real rc2 = sizeof(Real) == 4 ? (Real)cP.rc2f : (Real)cP.rc2;
+        const Real epsRF = (Real)cP.epsRFInvrc3;
+        for (int k = 0; k < cnt; ++k) {
+            uint32_t e = __ldg(&nbr[(int64_t)k * cap + i]);
+            int64_t j = e & MD_INDEX_MASK;
+            uint32_t code = e >> MD_CODE_SHIFT;
+            Real md[3];
+            if (sizeof(Real) == 4) {
+                float4 pj = __ldg(&xlf[j]);
+                md[0] = (pi[0] - (Real)pj.x) - soff[code][0];
+                md[1] = (pi[1] - (Real)pj.y) - soff[code][1];
+                md[2] = (pi[2] - (Real)pj.z) - soff[code][2];
+            } else {
+                double shf[3];
+                image_shift(S.home[i], code, shf);
+                md[0] = pi[0] - (S.rx[j] + shf[0]);
+                md[1] = pi[1] - (S.ry[j] + shf[1]);
+                md[2] = pi[2] - (S.rz[j] + shf[2]);
+            }
+            Real r2 = md[0] * md[0] + (md[1] * md[1] + md[2] * md[2]);
+            bool lj_on = r2 < rclj2, el_on = r2 < rc2;
+            if (sizeof(Real) == 4) {
+                bool bl = r2 > (Real)cP.band_lo_lj && r2 < (Real)cP.band_hi_lj;
+                bool be = r2 > (Real)cP.band_lo && r2 < (Real)cP.band_hi;
+                if (bl || be) {
+                    double r2d = fp64_r2(S, i, j, code);
+                    if (bl) lj_on = r2d < cP.rclj2;
+                    if (be) el_on = r2d < cP.rc2;
+                }
+            }
+            if (!lj_on && !el_on) continue;
+            const int cj = S.comp[j];
+            const CompDev& B = cP.comp[cj];
+            const bool macro = j > i;
+            if (el_on && macro) cnt_pairs[0] += 1.0;
+            for (int a = 0; a < A.ns; ++a) {
+                const int ka = A.kind[a];
+                if (ka == SK_LJ && !lj_on) continue;
+                if (ka != SK_LJ && !el_on) continue;
+                Real da[3], ea[3] = {0, 0, 0};
+                for (int c = 0; c < 3; ++c) da[c] = sd[((int64_t)i * stride + a) * 3 + c];
+                if (ka >= SK_DIPOLE)
+                    for (int c = 0; c < 3; ++c) ea[c] = se[((int64_t)i * stride + a) * 3 + c];
+                Real fa[3] = {0, 0, 0}, ta[3] = {0, 0, 0};
+                for (int b = 0; b < B.ns; ++b) {
+                    const int kb = B.kind[b];
+                    if ((ka == SK_LJ) != (kb == SK_LJ)) continue;
+                    Real db[3], eb[3] = {0, 0, 0};
+                    for (int c = 0; c < 3; ++c) db[c] = sd[((int64_t)j * stride + b) * 3 + c];
+                    if (kb >= SK_DIPOLE)
+                        for (int c = 0; c < 3; ++c) eb[c] = se[((int64_t)j * stride + b) * 3 + c];
+                    Real dsite[3] = {md[0] + (da[0] - db[0]), md[1] + (da[1] - db[1]), md[2] + (da[2] - db[2])};
+                    Real f[3], Vp[3], T[3] = {0, 0, 0}, u = 0, urf = 0;
+                    int kind;
+                    if (ka == SK_LJ) {
+                        int ga = A.ljoff + a, gb = B.ljoff + b;
+                        Real s2r = dsite[0] * dsite[0] + (dsite[1] * dsite[1] + dsite[2] * dsite[2]);
+                        lj_pair<Real>(dsite, md, s2r, (Real)cP.eps24[ga * cP.nlj + gb], (Real)cP.sig2[ga * cP.nlj + gb],
+                                      (Real)cP.shift6[ga * cP.nlj + gb], f, Vp, u);
+                        if (macro) u6.add(u);
+                        kind = 0;
+                    } else {
+                        kind = multipole_pair<Real>(ka, kb, dsite, md, (Real)A.p[a], ea, (Real)B.p[b], eb, epsRF, f, Vp,
+                                                    T, u, urf);
+                        if (macro) { ux.add(u); rf.add(urf); }
+                    }
+                    for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
+                    for (int c = 0; c < 3; ++c) { F[c].add(f[c]); V[c].add(Vp[c]); }
+                    if (macro) {
+                        vir.add(Vp[0] + Vp[1] + Vp[2]);
+                        cnt_pairs[1 + kind] += 1.0;
+                    }
+                }
+                // torque of the site forces about the centre plus the multipole torque
+                Real cx = da[1] * fa[2] - da[2] * fa[1];
+                Real cy = da[2] * fa[0] - da[0] * fa[2];
+                Real cz = da[0] * fa[1] - da[1] * fa[0];
+                M[0].add(cx + ta[0]); M[1].add(cy + ta[1]); M[2].add(cz + ta[2]);
+            }
+        }
+        S.Fx[i] = F[0].value(); S.Fy[i] = F[1].value(); S.Fz[i] = F[2].value();
+        S.Mx[i] = M[0].value(); S.My[i] = M[1].value(); S.Mz[i] = M[2].value();
+        S.Vx[i] = 0.5 * V[0].value(); S.Vy[i] = 0.5 * V[1].value(); S.Vz[i] = 0.5 * V[2].value();
+    }
+    double* P = partials + (size_t)blockIdx.x * NPART;
+    double t;
+    t = block_sum(u6.value(), sh); if (threadIdx.x == 0) P[0] = t;
+    t = block_sum(ux.value(), sh); if (threadIdx.x == 0) P[1] = t;
+    t = block_sum(vir.value(), sh); if (threadIdx.x == 0) P[2] = t;
+    t = block_sum(-rf.value(), sh); if (threadIdx.x == 0) P[3] = t;
+    for (int s = 0; s < 8; ++s) {
+        t = block_sum(cnt_pairs[s], sh);
+        if (threadIdx.x == 0) P[4 + s] = t;
+    }
+}
+
+// ------------------------------------------------------------------ integration
+// FullMolecule::upd_preF; afterwards the FP32 local coordinates and the
+// displacement since the last list build (for the rebuild test).
+__global__ void k_pre(State S, double dt, float4* xlf, const double* rref, unsigned* disp_max) {
+    __shared__ float smax[8];
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float d2 = 0.f;
+    if (i < S.n) {
+        const CompDev& C = cP.comp[S.comp[i]];
+        double dt_halve = .5 * dt;
+        double dtInv2m = dt_halve / C.m;
+        double vx = S.vx[i] + dtInv2m * S.Fx[i];
+        double vy = S.vy[i] + dtInv2m * S.Fy[i];
+        double vz = S.vz[i] + dtInv2m * S.Fz[i];
+        double rx = S.rx[i] + dt * vx, ry = S.ry[i] + dt * vy, rz = S.rz[i] + dt * vz;
+        S.vx[i] = vx; S.vy[i] = vy; S.vz[i] = vz;
+        S.rx[i] = rx; S.ry[i] = ry; S.rz[i] = rz;
+        if (!C.skip_rot) {
+            double q[4] = {S.qw[i], S.qx[i], S.qy[i], S.qz[i]};
+            double L[3] = {S.Lx[i], S.Ly[i], S.Lz[i]};
+            double w[3];
+            qrotinv(q[0], q[1], q[2], q[3], L, w);
+            for (int d = 0; d < 3; ++d) w[d] *= C.invI[d];
+            double qh[4];
+            qh[0] = .5 * (-q[1] * w[0] - q[2] * w[1] - q[3] * w[2]);
+            qh[1] = .5 * (q[0] * w[0] - q[3] * w[1] + q[2] * w[2]);
+            qh[2] = .5 * (q[3] * w[0] + q[0] * w[1] - q[1] * w[2]);
+            qh[3] = .5 * (-q[2] * w[0] + q[1] * w[1] + q[0] * w[2]);
+            for (int e = 0; e < 4; ++e) qh[e] = qh[e] * dt_halve + q[e];
+            double qc = 1. / sqrt(qh[0] * qh[0] + qh[1] * qh[1] + qh[2] * qh[2] + qh[3] * qh[3]);
+            for (int e = 0; e < 4; ++e) qh[e] *= qc;
+            L[0] += dt_halve * S.Mx[i]; L[1] += dt_halve * S.My[i]; L[2] += dt_halve * S.Mz[i];
+            qrotinv(qh[0], qh[1], qh[2], qh[3], L, w);
+            for (int d = 0; d < 3; ++d) w[d] *= C.invI[d];
+            double qi[4];
+            qi[0] = .5 * (-qh[1] * w[0] - qh[2] * w[1] - qh[3] * w[2]);
+            qi[1] = .5 * (qh[0] * w[0] - qh[3] * w[1] + qh[2] * w[2]);
+            qi[2] = .5 * (qh[3] * w[0] + qh[0] * w[1] - qh[1] * w[2]);
+            qi[3] = .5 * (-qh[2] * w[0] + qh[1] * w[1] + qh[0] * w[2]);
+            for (int e = 0; e < 4; ++e) q[e] += qi[e] * dt;
+            qc = 1. / sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+            for (int e = 0; e < 4; ++e) q[e] *= qc;
+            S.qw[i] = q[0]; S.qx[i] = q[1]; S.qy[i] = q[2]; S.qz[i] = q[3];
+            S.Lx[i] = L[0]; S.Ly[i] = L[1]; S.Lz[i] = L[2];
+        }
+        make_local<float4>(S, i, xlf);
+        float ddx = (float)(rx - rref[3 * i]), ddy = (float)(ry - rref[3 * i + 1]), ddz = (float)(rz - rref[3 * i + 2]);
+        d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+    }
+    for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, o));
+    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = d2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, smax[w]);
+        atomicMax(disp_max, __float_as_uint(m));
+    }
+}
+
+// Rebuild when two molecules may have approached by more than the skin.
+__global__ void k_check_rebuild(unsigned* disp_max, unsigned* need, float half_skin2, int force,
+                                unsigned long long* nrebuild) {
+    float m = __uint_as_float(*disp_max);
+    *need = (force || m > half_skin2) ? 1u : 0u;
+    if (*need) {
+        *disp_max = 0u;
+        *nrebuild += 1ull;
+    }
+}
+
+__global__ void k_sum_int(const int* a, int64_t n, unsigned long long* out) {
+    unsigned long long s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += (unsigned long long)a[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+// FullMolecule::upd_postF with the Leapfrog sums.
+__global__ void k_post(State S, double dt, double* partials) {
+    __shared__ double sh[32];
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double mv2 = 0.0, iw2 = 0.0, rot = 0.0, one = 0.0;
+    if (i < S.n) {
+        const CompDev& C = cP.comp[S.comp[i]];
+        double dt_halve = 0.5 * dt;
+        double dtInv2m = dt_halve / C.m;
+        double v[3] = {S.vx[i], S.vy[i], S.vz[i]};
+        double F[3] = {S.Fx[i], S.Fy[i], S.Fz[i]};
+        double L[3] = {S.Lx[i], S.Ly[i], S.Lz[i]};
+        double M[3] = {S.Mx[i], S.My[i], S.Mz[i]};
+        double v2 = 0.;
+        for (int d = 0; d < 3; ++d) {
+            v[d] += dtInv2m * F[d];
+            v2 += v[d] * v[d];
+            L[d] += dt_halve * M[d];
+        }
+        mv2 = C.m * v2;
+        S.vx[i] = v[0]; S.vy[i] = v[1]; S.vz[i] = v[2];
+        if (!C.skip_rot) {
+            S.Lx[i] = L[0]; S.Ly[i] = L[1]; S.Lz[i] = L[2];
+            double w[3];
+            qrotinv(S.qw[i], S.qx[i], S.qy[i], S.qz[i], L, w);
+            for (int d = 0; d < 3; ++d) {
+                w[d] *= C.invI[d];
+                iw2 += C.I[d] * w[d] * w[d];
+            }
+        }
+        rot = C.rot_dof;
+        one = 1.0;
+    }
+    double* P = partials + (size_t)blockIdx.x * NPART;
+    double t;
+    t = block_sum(mv2, sh); if (threadIdx.x == 0) P[12] = t;
+    t = block_sum(iw2, sh); if (threadIdx.x == 0) P[13] = t;
+    t = block_sum(one, sh); if (threadIdx.x == 0) P[14] = t;
+    t = block_sum(rot, sh); if (threadIdx.x == 0) P[15] = t;
+}
+
+#include "md_api.inc"

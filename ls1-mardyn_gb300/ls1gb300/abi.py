@@ -64,6 +64,12 @@ class MdStepRecord(C.Structure):
     _fields_ = [("upot", C.c_double), ("virial", C.c_double), ("summv2", C.c_double), ("sumIw2", C.c_double)]
 
 
+class MdKernelTimes(C.Structure):
+    _fields_ = [("force_ms", C.c_double), ("pre_ms", C.c_double), ("post_ms", C.c_double),
+                ("rebuild_ms", C.c_double), ("mean_candidates", C.c_double), ("rebuilds", C.c_int64),
+                ("launches_per_step", C.c_int32), ("reserved", C.c_int32)]
+
+
 def dptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 

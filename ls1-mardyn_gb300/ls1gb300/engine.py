@@ -1,0 +1,200 @@
+"""ctypes binding of libls1gb300.so and a Python mirror of the reference's
+container/integrator interface for this path.
+
+``Engine`` is one ``md_ctx`` (one box).  ``GpuLinkedCells`` and
+``GpuLeapfrog`` mirror the method names and call order of the reference's
+``ParticleContainer`` (src/particleContainer/ParticleContainer.h:69-296) and
+``Integrator``/``Leapfrog`` (src/integrators/Integrator.h:32-84,
+src/integrators/Leapfrog.cpp:32-147), so a driver loop reads like
+``Simulation::simulateOneTimestep`` (src/Simulation.cpp:1076-1300).
+
+There is no CPU fallback: if the CUDA library is missing the constructor
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import abi
+from .phasespace import PhaseSpace
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "libls1gb300.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "ls1gb300.h")
+_lib = None
+
+PRECISION = {"fp64": abi.MD_PREC_FP64, "mixed": abi.MD_PREC_MIXED}
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{abi.ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the engine library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} missing: build it with ls1-mardyn_gb300/build.py")
+    L = C.CDLL(path)
+    vp, i64, i32, dp, d = C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double), C.c_double
+    L.md_create.argtypes = [C.POINTER(vp), C.POINTER(abi.MdConfig)]
+    L.md_destroy.argtypes = [vp]
+    L.md_last_error.argtypes = [vp]
+    L.md_last_error.restype = C.c_char_p
+    L.md_set_components.argtypes = [vp, C.POINTER(abi.MdComponent), i32, dp]
+    L.md_upload_molecules.argtypes = [vp, i64, vp, vp, dp, dp, dp, dp]
+    L.md_download_molecules.argtypes = [vp, i64] + [vp] * 9
+    L.md_rebin_and_halo.argtypes = [vp, C.POINTER(abi.MdBinStats)]
+    L.md_get_cell_assignment.argtypes = [vp, i64, vp]
+    L.md_compute_forces.argtypes = [vp, C.POINTER(abi.MdForcesOut)]
+    L.md_integrate_pre.argtypes = [vp, d]
+    L.md_integrate_post.argtypes = [vp, d, C.POINTER(abi.MdKineticOut)]
+    L.md_run.argtypes = [vp, d, i32, C.POINTER(abi.MdStepRecord)]
+    L.md_sync.argtypes = [vp]
+    L.md_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.md_time_kernels.argtypes = [vp, i32, C.POINTER(abi.MdKernelTimes)]
+    _lib = L
+    return L
+
+
+class Engine:
+    """One box on the GPU behind the C ABI."""
+
+    def __init__(self, ps: PhaseSpace, rc: float, rc_lj: Optional[float] = None,
+                 periodic: Sequence[int] = (1, 1, 1), precision: str = "fp64", skin: float = 0.0,
+                 device: int = 0, capacity: int = 0):
+        self.L = load_library()
+        self.ps = ps
+        self.cfg = abi.make_config(ps.box, rc, rc if rc_lj is None else rc_lj, ps.eps_rf, periodic,
+                                   PRECISION[precision], capacity, skin, device)
+        self.h = C.c_void_p()
+        self._check(self.L.md_create(C.byref(self.h), C.byref(self.cfg)), "md_create")
+        self.tables = abi.ComponentTables(ps.components, ps.mixing)
+        self._check(self.L.md_set_components(self.h, self.tables.array, self.tables.ncomp, self.tables.mixing),
+                    "md_set_components")
+        self.upload(ps)
+
+    def _check(self, rc: int, what: str):
+        if rc != abi.MD_OK:
+            msg = self.L.md_last_error(self.h).decode() if self.h else ""
+            raise EngineError(rc, f"{what}: {msg}")
+
+    def upload(self, ps: PhaseSpace):
+        ids, comp, r, v, q, Lm = abi.molecule_arrays(ps)
+        self.n = ps.n
+        self._check(self.L.md_upload_molecules(self.h, ps.n, ids.ctypes.data, comp.ctypes.data, abi.dptr(r),
+                                               abi.dptr(v), abi.dptr(q), abi.dptr(Lm)), "md_upload_molecules")
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.md_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def rebin(self) -> abi.MdBinStats:
+        st = abi.MdBinStats()
+        self._check(self.L.md_rebin_and_halo(self.h, C.byref(st)), "md_rebin_and_halo")
+        return st
+
+    def cells(self) -> np.ndarray:
+        out = np.zeros(self.n, np.int64)
+        self._check(self.L.md_get_cell_assignment(self.h, self.n, out.ctypes.data), "md_get_cell_assignment")
+        return out
+
+    def forces(self) -> abi.MdForcesOut:
+        fo = abi.MdForcesOut()
+        self._check(self.L.md_compute_forces(self.h, C.byref(fo)), "md_compute_forces")
+        return fo
+
+    def pre(self, dt: float):
+        self._check(self.L.md_integrate_pre(self.h, dt), "md_integrate_pre")
+
+    def post(self, dt: float) -> abi.MdKineticOut:
+        ko = abi.MdKineticOut()
+        self._check(self.L.md_integrate_post(self.h, dt, C.byref(ko)), "md_integrate_post")
+        return ko
+
+    def run(self, dt: float, nsteps: int, record: bool = True) -> Optional[np.ndarray]:
+        rec = (abi.MdStepRecord * max(nsteps, 1))() if record else None
+        self._check(self.L.md_run(self.h, dt, nsteps, rec), "md_run")
+        if not record:
+            return None
+        return np.array([[x.upot, x.virial, x.summv2, x.sumIw2] for x in rec[:nsteps]])
+
+    def sync(self):
+        self._check(self.L.md_sync(self.h), "md_sync")
+
+    def stream(self) -> int:
+        """cudaStream_t of the context as an integer (for torch.cuda.ExternalStream)."""
+        s = C.c_void_p()
+        self._check(self.L.md_get_stream(self.h, C.byref(s)), "md_get_stream")
+        return s.value or 0
+
+    def time_kernels(self, reps: int = 10) -> abi.MdKernelTimes:
+        t = abi.MdKernelTimes()
+        self._check(self.L.md_time_kernels(self.h, reps, C.byref(t)), "md_time_kernels")
+        return t
+
+    def molecules(self) -> dict:
+        n = self.n
+        out = dict(ids=np.zeros(n, np.uint64), comp=np.zeros(n, np.int32), r=np.zeros((n, 3)), v=np.zeros((n, 3)),
+                   q=np.zeros((n, 4)), L=np.zeros((n, 3)), F=np.zeros((n, 3)), M=np.zeros((n, 3)),
+                   Vi=np.zeros((n, 3)))
+        self._check(self.L.md_download_molecules(self.h, n, *(out[k].ctypes.data for k in
+                                                              ("ids", "comp", "r", "v", "q", "L", "F", "M", "Vi"))),
+                    "md_download_molecules")
+        return out
+
+
+class GpuLinkedCells:
+    """Mirror of the reference's ParticleContainer calls used on this path."""
+
+    def __init__(self, ps: PhaseSpace, cutoff: float, lj_cutoff: Optional[float] = None, **kw):
+        self.engine = Engine(ps, cutoff, lj_cutoff, **kw)
+        self._cutoff = cutoff
+
+    # ParticleContainer::update + DomainDecompBase::exchangeMolecules + updateMoleculeCaches
+    def update(self) -> abi.MdBinStats:
+        return self.engine.rebin()
+
+    # ParticleContainer::traverseCells(VectorizedCellProcessor&) + Simulation::updateForces
+    def traverseCells(self) -> abi.MdForcesOut:
+        return self.engine.forces()
+
+    def getNumberOfParticles(self) -> int:
+        return self.engine.n
+
+    def getCutoff(self) -> float:
+        return self._cutoff
+
+    def getCellIndexOfMolecules(self) -> np.ndarray:
+        return self.engine.cells()
+
+    def molecules(self) -> dict:
+        return self.engine.molecules()
+
+
+class GpuLeapfrog:
+    """Mirror of Leapfrog's state machine (Leapfrog.cpp:32-147)."""
+
+    def __init__(self, dt: float):
+        self.dt = dt
+
+    def eventNewTimestep(self, cells: GpuLinkedCells):
+        cells.engine.pre(self.dt)
+
+    def eventForcesCalculated(self, cells: GpuLinkedCells) -> abi.MdKineticOut:
+        return cells.engine.post(self.dt)

@@ -1,0 +1,74 @@
+"""The C-ABI library: it builds, loads without a GPU, exports every entry
+point declared in include/ls1gb300.h, and the ctypes structs match the C
+layouts (checked against a C program compiled from the header)."""
+import ctypes
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "ls1-mardyn_gb300"))
+import build as engine_build  # noqa: E402
+from ls1gb300 import abi  # noqa: E402
+
+HEADER = os.path.join(ROOT, "include", "ls1gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(md_\w+)\s*\(", text, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    path = engine_build.build()
+    return ctypes.CDLL(path)
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 12
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_struct_layouts_match_header():
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "ls1gb300.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu\n", sizeof(md_config), sizeof(md_component), sizeof(md_bin_stats),
+         sizeof(md_forces_out), sizeof(md_kinetic_out), sizeof(md_step_record));
+  printf("%zu %zu %zu\n", offsetof(md_config, skin), offsetof(md_component, inertia), offsetof(md_forces_out, site_pairs));
+  return 0;
+}
+'''
+    d = tempfile.mkdtemp()
+    with open(os.path.join(d, "t.c"), "w") as f:
+        f.write(src)
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), "-o", os.path.join(d, "t"), os.path.join(d, "t.c")],
+                   check=True)
+    out = subprocess.run([os.path.join(d, "t")], capture_output=True, text=True, check=True).stdout.split()
+    sizes = [int(x) for x in out]
+    assert sizes[:6] == [ctypes.sizeof(t) for t in (abi.MdConfig, abi.MdComponent, abi.MdBinStats,
+                                                    abi.MdForcesOut, abi.MdKineticOut, abi.MdStepRecord)]
+    assert sizes[6] == abi.MdConfig.skin.offset
+    assert sizes[7] == abi.MdComponent.inertia.offset
+    assert sizes[8] == abi.MdForcesOut.site_pairs.offset
+
+
+def test_create_without_gpu_fails_cleanly(lib):
+    """Without a visible GPU md_create returns MD_ERR_CUDA instead of crashing."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    lib.md_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(abi.MdConfig)]
+    h = ctypes.c_void_p()
+    cfg = abi.make_config((10.0, 10.0, 10.0), 2.5, 2.5, 1e10)
+    assert lib.md_create(ctypes.byref(h), ctypes.byref(cfg)) == abi.MD_ERR_CUDA
+    assert not h.value

@@ -1,0 +1,166 @@
+"""Parity of the CUDA engine (through the C ABI) with the reference's golden
+outputs and with the pinned C oracle.
+
+Tolerances:
+  * cell assignment, halo copy count, largest cell occupancy and the
+    interacting molecule / site pair counts: exact, in both precisions (the
+    mixed kernel re-decides pairs within 4e-6 relative of the cut-off in FP64);
+  * FP64 kernel: F, M, Vi and Upot/virial to 1e-10 relative to the largest
+    magnitude of the case (FMA contraction and summation order differ);
+  * mixed kernel: relative rms force error <= 1e-5 (the precision target
+    stated for this path), torques and virials <= 1e-4, Upot/virial 1e-5;
+  * NVE runs (md_run, CUDA graph): per-step Upot, virial, sum m v^2 and
+    sum I w^2 to 1e-8 relative (FP64), 1e-4 (mixed, 10-20 steps).
+"""
+import numpy as np
+import pytest
+
+import golden_io
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+FORCE_CASES = golden_io.names("ref_") + golden_io.names("per_")
+NVE_CASES = golden_io.names("nve_")
+
+
+@pytest.fixture(scope="module")
+def engine_mod():
+    import importlib
+    import sys
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, os.path.join(root, "ls1-mardyn_gb300"))
+    import build as eb
+    eb.build()
+    return importlib.import_module("ls1gb300.engine")
+
+
+def _by_id(ids):
+    return np.argsort(ids, kind="stable")
+
+
+def _rel_max(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _rel_rms(a, b):
+    return np.sqrt(((a - b) ** 2).sum(axis=1).mean()) / max(np.sqrt((b ** 2).sum(axis=1).mean()), 1e-300)
+
+
+def _engine(E, name, precision, skin=0.0):
+    ps, g = golden_io.load(name)
+    e = E.Engine(ps, g["rc"], g["rc_lj"], (1, 1, 1) if g["periodic"] else (0, 0, 0), precision=precision, skin=skin)
+    return ps, g, e
+
+
+@pytest.mark.parametrize("name", FORCE_CASES)
+def test_fp64_forces_match_reference(engine_mod, name):
+    ps, g, e = _engine(engine_mod, name, "fp64")
+    st = e.rebin()
+    assert list(st.cells) == list(g["grid"])
+    o = Oracle(ps, g["rc"], g["rc_lj"], (1, 1, 1) if g["periodic"] else (0, 0, 0))
+    ost = o.rebin()
+    assert st.n_halo == ost.n_halo
+    assert st.max_occupancy == ost.max_occupancy
+    fo = e.forces()
+    m = e.molecules()
+    a, b = _by_id(m["ids"]), _by_id(g["out_ids"])
+    assert np.array_equal(m["ids"][a], g["out_ids"][b])
+    assert np.array_equal(e.cells()[a], g["out_cell"][b])
+    for key in ("F", "M", "Vi"):
+        if np.abs(g[key]).max() > 1e-9:
+            assert _rel_max(m[key][a], g[key][b]) < 1e-10, key
+        else:
+            assert np.abs(m[key]).max() < 1e-9, key
+    for mine, ref in ((fo.upot, float(g["upot"])), (fo.virial, float(g["virial"]))):
+        assert abs(mine - ref) <= 1e-10 * max(1.0, abs(ref))
+    assert list(fo.site_pairs) == list(g["counts"][2::2].astype(np.int64))
+    ofo, _ = o.forces()
+    assert fo.mol_pairs == ofo.mol_pairs
+
+
+@pytest.mark.parametrize("name", FORCE_CASES)
+def test_mixed_forces_match_reference(engine_mod, name):
+    ps, g, e = _engine(engine_mod, name, "mixed")
+    e.rebin()
+    fo = e.forces()
+    m = e.molecules()
+    a, b = _by_id(m["ids"]), _by_id(g["out_ids"])
+    if np.abs(g["F"]).max() > 1e-9:
+        assert _rel_rms(m["F"][a], g["F"][b]) <= 1e-5
+    else:
+        assert np.abs(m["F"]).max() < 1e-4
+    for key in ("M", "Vi"):
+        if np.abs(g[key]).max() > 1e-9:
+            assert _rel_rms(m[key][a], g[key][b]) <= 1e-4, key
+    for mine, ref in ((fo.upot, float(g["upot"])), (fo.virial, float(g["virial"]))):
+        assert abs(mine - ref) <= 1e-5 * max(1.0, abs(ref))
+    assert list(fo.site_pairs) == list(g["counts"][2::2].astype(np.int64))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", NVE_CASES)
+def test_nve_matches_reference(engine_mod, name, precision):
+    ps, g = golden_io.load(name)
+    skin = 0.3 * g["rc"] if precision == "mixed" else 0.0
+    e = engine_mod.Engine(ps, g["rc"], g["rc_lj"], (1, 1, 1), precision=precision, skin=skin)
+    e.forces()
+    rec = e.run(float(g["dt"]), int(g["nsteps"]))
+    ref = g["steps"][1:, 1:]
+    tol = 1e-8 if precision == "fp64" else 1e-4
+    for col in range(4):
+        scale = max(np.abs(ref[:, col]).max(), 1e-300)
+        assert np.abs(rec[:, col] - ref[:, col]).max() <= tol * scale, col
+    if precision == "fp64" and "out_r" in g:
+        m = e.molecules()
+        a, b = _by_id(m["ids"]), _by_id(g["out_ids"])
+        for key, gk in (("r", "out_r"), ("v", "out_v"), ("q", "out_q"), ("L", "out_L")):
+            assert np.abs(m[key][a] - g[gk][b]).max() < 1e-7, key
+
+
+def test_skin_does_not_change_the_trajectory(engine_mod):
+    """The pair-candidate list with a skin finds exactly the pairs of the
+    rebuild-every-step schedule: FP64 runs with skin 0 and skin 0.4 agree."""
+    ps, g = golden_io.load("per_lj4000j")
+    runs = []
+    for skin in (0.0, 0.4):
+        e = engine_mod.Engine(ps, 2.5, 2.5, precision="fp64", skin=skin)
+        e.forces()
+        runs.append(e.run(0.002, 60))
+    assert np.abs(runs[0] - runs[1]).max() <= 1e-9 * np.abs(runs[0]).max()
+
+
+def test_step_by_step_equals_md_run(engine_mod):
+    """md_integrate_pre / md_compute_forces / md_integrate_post (the
+    Leapfrog/ParticleContainer mirror) equal the graph-captured md_run."""
+    ps, g = golden_io.load("per_lj500")
+    cells = engine_mod.GpuLinkedCells(ps, 2.5, precision="fp64", skin=0.3)
+    lf = engine_mod.GpuLeapfrog(0.002)
+    cells.traverseCells()
+    manual = []
+    for _ in range(12):
+        lf.eventNewTimestep(cells)
+        fo = cells.traverseCells()
+        ko = lf.eventForcesCalculated(cells)
+        manual.append([fo.upot, fo.virial, ko.summv2])
+    e = engine_mod.Engine(ps, 2.5, precision="fp64", skin=0.3)
+    e.forces()
+    rec = e.run(0.002, 12)
+    assert np.allclose(np.array(manual), rec[:, :3], rtol=1e-12, atol=0)
+
+
+def test_mixed_matches_fp64_at_scale(engine_mod):
+    """1CLJ N=32000 (the reference's small benchmark case): mixed-precision
+    forces within 1e-5 relative rms of the FP64 kernel, Upot within 1e-6."""
+    ps, g = golden_io.load("nve_lj32000")
+    rng = np.random.default_rng(3)
+    ps.r = ps.r + rng.uniform(-0.1, 0.1, ps.r.shape)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        e = engine_mod.Engine(ps, 2.5, precision=prec, skin=0.3)
+        fo = e.forces()
+        out[prec] = (e.molecules()["F"], fo)
+    assert _rel_rms(out["mixed"][0], out["fp64"][0]) <= 1e-5
+    assert abs(out["mixed"][1].upot - out["fp64"][1].upot) <= 1e-6 * abs(out["fp64"][1].upot)
+    assert out["mixed"][1].site_pairs[0] == out["fp64"][1].site_pairs[0]
