@@ -47,6 +47,8 @@ WORKLOADS = {
     # name: (generator, rc, dt, description)
     "lj4m": (lambda: psm.lj_fcc(100, 0.75, 0.9, seed=2024), 3.0, 0.002,
              "1CLJ fcc 100^3x4 = 4,000,000, rho*=0.75, T*=0.9, rc=3.0, dt=0.002"),
+    "lj1m": (lambda: psm.lj_fcc(63, 0.75, 0.9, seed=2024), 3.0, 0.002,
+             "1CLJ fcc 63^3x4 = 1,000,188, rho*=0.75, T*=0.9, rc=3.0, dt=0.002 (profiling size)"),
     "lj32k": (lambda: psm.lj_fcc(20, 0.8, 1.0, seed=1), 2.5, 0.002,
               "1CLJ fcc 20^3x4 = 32,000, rho*=0.8, T*=1.0, rc=2.5, dt=0.002"),
     "slab": (lambda: psm.lj_slab(91, 0.73, 0.02, 0.9, seed=2025), 3.0, 0.002,
@@ -54,7 +56,7 @@ WORKLOADS = {
     "mix1m": (lambda: psm.mixture(1_000_000, 18.0, 300.0, seed=2026), 1.0, 9.118e-5,
               "2CLJQ/1CLJD 50/50 mixture, N=1,000,188, n=18 nm^-3, T=300 K, rc=1 nm, RF eps=1e10, dt=1 fs"),
 }
-DEFAULT_SKIN = {"lj4m": 0.3, "lj32k": 0.3, "slab": 0.3, "mix1m": 0.1}
+DEFAULT_SKIN = {"lj4m": 0.3, "lj1m": 0.3, "lj32k": 0.3, "slab": 0.3, "mix1m": 0.1}
 FLOP_PER_PAIR_LJ = 39.0  # reference FlopCounter model: 31 per LJ site pair + 8 per molecule distance
 
 
@@ -150,7 +152,7 @@ class ClockSampler:
 def cpu_baseline(workload: str, budget_s: float = 12.0) -> dict:
     from oracle.oracle import Oracle
     gen, rc, dt, _ = WORKLOADS[workload]
-    if workload in ("lj4m", "slab"):
+    if workload in ("lj4m", "lj1m", "slab"):
         ps = psm.lj_fcc(14, 0.75, 0.9, seed=7)        # 10,976 molecules, same state point
         sample = "1CLJ fcc 14^3x4 = 10,976 molecules at the same rho*, T*, rc, dt"
     elif workload == "lj32k":

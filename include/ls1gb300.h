@@ -151,6 +151,24 @@ int md_integrate_post(md_ctx* ctx, double dt, md_kinetic_out* out);
  * steps; rec (nsteps entries, may be NULL) receives the per-step sums. */
 int md_run(md_ctx* ctx, double dt, int32_t nsteps, md_step_record* rec);
 
+/* Adjoint of the force field at the current state (after md_compute_forces).
+ * No counterpart in the reference, which has no gradients.  With upstream
+ * gradients gU = dL/dUpot and gW = dL/dvirial (Upot and virial as reported by
+ * md_compute_forces) and optionally gF (n x 3, dL/dF per molecule in upload
+ * order, or NULL), it returns
+ *   grad_r (n x 3, upload order, may be NULL):
+ *       gU dUpot/dr + gW dvirial/dr + pair Hessian-vector products with gF
+ *       (positions only; orientations held fixed),
+ *   grad_params (nparam, may be NULL): gU dUpot/dp + gW dvirial/dp for the
+ *       site parameters in the order: components in order, sites in the order
+ *       LJ, charge, dipole, quadrupole; an LJ centre contributes (eps, sigma),
+ *       a charge q, a dipole |mu|, a quadrupole |Q|.
+ * nparam must equal that count (sum over components of 2 n_lj + n_charge +
+ * n_dipole + n_quadrupole, at most 128).  Pairs are recomputed from the
+ * pair-candidate list; nothing of the forward pass is stored. */
+int md_adjoint(md_ctx* ctx, double gU, double gW, const double* gF, double* grad_r, double* grad_params,
+               int32_t nparam);
+
 /* Wait for all work of the context. */
 int md_sync(md_ctx* ctx);
 

@@ -172,6 +172,8 @@ __device__ int64_t ref_cell_of_point(const double* point, const double* border, 
         for (int d = 0; d < 3; ++d) {
             if (p[d] < border[d * bstride + ci[d]]) ci[d]--;
             else if (p[d] >= border[d * bstride + ci[d] + 1]) ci[d]++;
+            // points outside the halo box (the reference asserts on these) stay in range
+            ci[d] = max(0, min(ci[d], cP.rcpd[d] - 1));
         }
     }
     return ((int64_t)ci[2] * cP.rcpd[1] + ci[1]) * cP.rcpd[0] + ci[0];
@@ -281,17 +283,38 @@ __global__ void k_list_scatter(int64_t n, const int* mcell, int* cursor, int* pe
     perm[p] = (int)i;
 }
 
-// Deterministic order inside each cell: sort the slot indices of the cell.
+// Deterministic order inside each cell: one warp per cell ranks the cell's
+// slot indices (the atomic scatter leaves them in arbitrary order) and writes
+// them back sorted.  Cells of up to 64 molecules are ranked in registers;
+// larger cells fall back to a serial insertion sort by lane 0.
 __global__ void k_cell_sort(const int* start, int ncells, int* perm, const unsigned* need) {
     if (!*need) return;
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
     if (c >= ncells) return;
-    int b = start[c], e = start[c + 1];
-    for (int k = b + 1; k < e; ++k) {
-        int v = perm[k];
-        int m = k - 1;
-        while (m >= b && perm[m] > v) { perm[m + 1] = perm[m]; --m; }
-        perm[m + 1] = v;
+    int b = start[c], e = start[c + 1], m = e - b;
+    if (m <= 1) return;
+    if (m <= 64) {
+        int v0 = lane < m ? perm[b + lane] : 0x7fffffff;
+        int v1 = lane + 32 < m ? perm[b + lane + 32] : 0x7fffffff;
+        int r0 = 0, r1 = 0;
+        for (int t = 0; t < 32; ++t) {
+            int a0 = __shfl_sync(0xffffffffu, v0, t), a1 = __shfl_sync(0xffffffffu, v1, t);
+            r0 += (a0 < v0) + (a1 < v0);
+            r1 += (a0 < v1) + (a1 < v1);
+        }
+        __syncwarp();
+        if (lane < m) perm[b + r0] = v0;
+        if (lane + 32 < m) perm[b + r1] = v1;
+        return;
+    }
+    if (lane == 0) {
+        for (int k = b + 1; k < e; ++k) {
+            int v = perm[k];
+            int q = k - 1;
+            while (q >= b && perm[q] > v) { perm[q + 1] = perm[q]; --q; }
+            perm[q + 1] = v;
+        }
     }
 }
 
@@ -447,20 +470,21 @@ __global__ void __launch_bounds__(256) k_force_lj(State S, const float4* xlf, co
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     typename Acc<Real>::type fx, fy, fz, vx, vy, vz, up, vir;
     fx.init(); fy.init(); fz.init(); vx.init(); vy.init(); vz.init(); up.init(); vir.init();
-    double npairs = 0.0, nmol = 0.0;
+    int npairs = 0, nmol = 0;
     if (i < S.n) {
-        const int ci = S.comp[i];
+        float4 p4 = xlf[i];
+        const int ci = __float_as_int(p4.w);
         const int gi = cP.comp[ci].ljoff;
         Real pix, piy, piz;
         if (sizeof(Real) == 4) {
-            float4 p = xlf[i];
-            pix = p.x; piy = p.y; piz = p.z;
+            pix = p4.x; piy = p4.y; piz = p4.z;
         } else {
             pix = S.rx[i]; piy = S.ry[i]; piz = S.rz[i];
         }
         const int cnt = nnb[i];
         const Real rclj2 = sizeof(Real) == 4 ? (Real)cP.rclj2f : (Real)cP.rclj2;
         const Real rc2 = sizeof(Real) == 4 ? (Real)cP.rc2f : (Real)cP.rc2;
+        const bool one_comp = cP.ncomp == 1;
         Real e24 = (Real)cP.eps24[gi * cP.nlj + gi], s2 = (Real)cP.sig2[gi * cP.nlj + gi];
         Real sh6 = (Real)cP.shift6[gi * cP.nlj + gi];
         int cur = gi;
@@ -468,9 +492,9 @@ __global__ void __launch_bounds__(256) k_force_lj(State S, const float4* xlf, co
             uint32_t e = __ldg(&nbr[(int64_t)k * cap + i]);
             int64_t j = e & MD_INDEX_MASK;
             uint32_t code = e >> MD_CODE_SHIFT;
+            float4 pj = __ldg(&xlf[j]);
             Real dx, dy, dz;
             if (sizeof(Real) == 4) {
-                float4 pj = __ldg(&xlf[j]);
                 dx = (pix - (Real)pj.x) - soff[code][0];
                 dy = (piy - (Real)pj.y) - soff[code][1];
                 dz = (piz - (Real)pj.z) - soff[code][2];
@@ -492,24 +516,27 @@ __global__ void __launch_bounds__(256) k_force_lj(State S, const float4* xlf, co
                     if (be) in_rc = r2d < cP.rc2;
                 }
             }
-            if (in_rc && j > i) nmol += 1.0;
+            const bool macro = j > i;
+            nmol += (in_rc && macro) ? 1 : 0;
             if (!in) continue;
-            const int gj = cP.comp[S.comp[j]].ljoff;
-            if (gj != cur) {
-                cur = gj;
-                e24 = (Real)cP.eps24[gi * cP.nlj + gj];
-                s2 = (Real)cP.sig2[gi * cP.nlj + gj];
-                sh6 = (Real)cP.shift6[gi * cP.nlj + gj];
+            if (!one_comp) {
+                const int gj = cP.comp[__float_as_int(pj.w)].ljoff;
+                if (gj != cur) {
+                    cur = gj;
+                    e24 = (Real)cP.eps24[gi * cP.nlj + gj];
+                    s2 = (Real)cP.sig2[gi * cP.nlj + gj];
+                    sh6 = (Real)cP.shift6[gi * cP.nlj + gj];
+                }
             }
             Real f[3], V[3], u;
             const Real d[3] = {dx, dy, dz};
             lj_pair<Real>(d, d, r2, e24, s2, sh6, f, V, u);
             fx.add(f[0]); fy.add(f[1]); fz.add(f[2]);
             vx.add(V[0]); vy.add(V[1]); vz.add(V[2]);
-            if (j > i) {
+            if (macro) {
                 up.add(u);
                 vir.add(V[0] + V[1] + V[2]);
-                npairs += 1.0;
+                ++npairs;
             }
         }
         S.Fx[i] = fx.value(); S.Fy[i] = fy.value(); S.Fz[i] = fz.value();
@@ -520,9 +547,9 @@ __global__ void __launch_bounds__(256) k_force_lj(State S, const float4* xlf, co
     double t;
     t = block_sum(up.value(), sh); if (threadIdx.x == 0) P[0] = t;
     t = block_sum(vir.value(), sh); if (threadIdx.x == 0) P[2] = t;
-    t = block_sum(npairs, sh);
+    t = block_sum((double)npairs, sh);
     if (threadIdx.x == 0) { P[1] = 0.0; P[3] = 0.0; P[5] = t; for (int s = 6; s < 12; ++s) P[s] = 0.0; }
-    t = block_sum(nmol, sh);
+    t = block_sum((double)nmol, sh);
     if (threadIdx.x == 0) P[4] = t;
 }
 
@@ -547,7 +574,7 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
     typename Acc<Real>::type F[3], M[3], V[3], u6, ux, vir, rf;
     for (int e = 0; e < 3; ++e) { F[e].init(); M[e].init(); V[e].init(); }
     u6.init(); ux.init(); vir.init(); rf.init();
-    double cnt_pairs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int cnt_pairs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (i < S.n) {
         const int ci = S.comp[i];
         const CompDev& A = cP.comp[ci];
@@ -594,7 +621,7 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
             const int cj = S.comp[j];
             const CompDev& B = cP.comp[cj];
             const bool macro = j > i;
-            if (el_on && macro) cnt_pairs[0] += 1.0;
+            if (el_on && macro) cnt_pairs[0] += 1;
             for (int a = 0; a < A.ns; ++a) {
                 const int ka = A.kind[a];
                 if (ka == SK_LJ && !lj_on) continue;
@@ -630,7 +657,7 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
                     for (int c = 0; c < 3; ++c) { F[c].add(f[c]); V[c].add(Vp[c]); }
                     if (macro) {
                         vir.add(Vp[0] + Vp[1] + Vp[2]);
-                        cnt_pairs[1 + kind] += 1.0;
+                        cnt_pairs[1 + kind] += 1;
                     }
                 }
                 // torque of the site forces about the centre plus the multipole torque
@@ -651,7 +678,7 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
     t = block_sum(vir.value(), sh); if (threadIdx.x == 0) P[2] = t;
     t = block_sum(-rf.value(), sh); if (threadIdx.x == 0) P[3] = t;
     for (int s = 0; s < 8; ++s) {
-        t = block_sum(cnt_pairs[s], sh);
+        t = block_sum((double)cnt_pairs[s], sh);
         if (threadIdx.x == 0) P[4 + s] = t;
     }
 }
@@ -775,4 +802,5 @@ __global__ void k_post(State S, double dt, double* partials) {
     t = block_sum(rot, sh); if (threadIdx.x == 0) P[15] = t;
 }
 
+#include "md_adjoint.inc"
 #include "md_api.inc"

@@ -60,6 +60,7 @@ def load_library(path: str = LIB_PATH):
     L.md_run.argtypes = [vp, d, i32, C.POINTER(abi.MdStepRecord)]
     L.md_sync.argtypes = [vp]
     L.md_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.md_adjoint.argtypes = [vp, d, d, vp, vp, vp, i32]
     L.md_time_kernels.argtypes = [vp, i32, C.POINTER(abi.MdKernelTimes)]
     _lib = L
     return L
@@ -147,6 +148,21 @@ class Engine:
         t = abi.MdKernelTimes()
         self._check(self.L.md_time_kernels(self.h, reps, C.byref(t)), "md_time_kernels")
         return t
+
+    def param_count(self) -> int:
+        return sum(2 * len(c.lj) + len(c.charges) + len(c.dipoles) + len(c.quadrupoles) for c in self.ps.components)
+
+    def adjoint(self, gU: float, gW: float, gF: Optional[np.ndarray] = None):
+        """(grad_r, grad_params) of gU*Upot + gW*virial (+ sum gF.F) at the
+        current state; see md_adjoint in include/ls1gb300.h for the order of
+        the parameters."""
+        gr = np.zeros((self.n, 3))
+        npar = self.param_count()
+        gp = np.zeros(max(npar, 1))
+        gFa = None if gF is None else np.ascontiguousarray(gF, dtype=np.float64)
+        self._check(self.L.md_adjoint(self.h, float(gU), float(gW), None if gFa is None else gFa.ctypes.data,
+                                      gr.ctypes.data, gp.ctypes.data, npar), "md_adjoint")
+        return gr, gp[:npar]
 
     def molecules(self) -> dict:
         n = self.n

@@ -69,10 +69,10 @@ def test_fp64_forces_match_reference(engine_mod, name):
     assert np.array_equal(m["ids"][a], g["out_ids"][b])
     assert np.array_equal(e.cells()[a], g["out_cell"][b])
     for key in ("F", "M", "Vi"):
-        if np.abs(g[key]).max() > 1e-9:
-            assert _rel_max(m[key][a], g[key][b]) < 1e-10, key
-        else:
-            assert np.abs(m[key]).max() < 1e-9, key
+        # forces that cancel to rounding level (ForceCalculationTestF0) are
+        # compared in absolute terms, as the reference's own test does
+        scale = max(np.abs(g[key]).max(), 1.0)
+        assert np.abs(m[key][a] - g[key][b]).max() <= 1e-10 * scale, key
     for mine, ref in ((fo.upot, float(g["upot"])), (fo.virial, float(g["virial"]))):
         assert abs(mine - ref) <= 1e-10 * max(1.0, abs(ref))
     assert list(fo.site_pairs) == list(g["counts"][2::2].astype(np.int64))
@@ -87,10 +87,10 @@ def test_mixed_forces_match_reference(engine_mod, name):
     fo = e.forces()
     m = e.molecules()
     a, b = _by_id(m["ids"]), _by_id(g["out_ids"])
-    if np.abs(g["F"]).max() > 1e-9:
+    if np.abs(g["F"]).max() > 1e-6:
         assert _rel_rms(m["F"][a], g["F"][b]) <= 1e-5
     else:
-        assert np.abs(m["F"]).max() < 1e-4
+        assert np.abs(m["F"] - g["F"]).max() < 1e-4
     for key in ("M", "Vi"):
         if np.abs(g[key]).max() > 1e-9:
             assert _rel_rms(m[key][a], g[key][b]) <= 1e-4, key
