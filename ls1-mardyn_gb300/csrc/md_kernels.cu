@@ -42,7 +42,7 @@ __constant__ Params cP;
 
 struct Scratch {
     // reductions
-    double* partials;       // [nblocks_max * NPART]
+    double* partials;       // [NPART][pstride], slot-major per-warp partials
     double* result;         // finalize output (NPART doubles)
     md_step_record* records;
     int* step;              // step counter for md_run records
@@ -56,9 +56,20 @@ struct Scratch {
 // slots: 0 upot6lj 1 upotXpoles 2 virial 3 myRF 4 mol_pairs 5..11 site pairs 12 summv2 13 sumIw2 14 n 15 rotdof
 
 // ------------------------------------------------------------------ reductions
+// Every kernel that contributes to the global sums writes, per warp of its
+// grid, one partial per slot into a slot-major array partials[slot * pstride
+// + warp]; all warps of the grid write (zeros where they own no molecule), so
+// nothing needs clearing.  k_finalize sums each slot in a fixed order
+// (deterministic) with one block per slot.
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
+}
+
+__device__ __forceinline__ void warp_partial(double* partials, int pstride, int slot, double v) {
+    v = warp_sum(v);
+    if ((threadIdx.x & 31) == 0)
+        partials[(size_t)slot * pstride + ((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5)] = v;
 }
 
 // Sum `v` over the block (blockDim multiple of 32, <= 1024); result valid in thread 0.
@@ -77,31 +88,26 @@ __device__ double block_sum(double v, double* sh) {
     return r;
 }
 
-__global__ void k_zero_partials(double* partials, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) partials[i] = 0.0;
+// slots 0..11 come from the force kernel (nw_force warps), 12..15 from the
+// post-force half step (nw_post warps); a count of 0 leaves a slot at 0.
+__global__ void k_finalize(const double* partials, int pstride, int nw_force, int nw_post, double* result) {
+    __shared__ double sh[32];
+    const int s = blockIdx.x;
+    const int nw = s < 12 ? nw_force : nw_post;
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nw; b += blockDim.x) v += partials[(size_t)s * pstride + b];
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) result[s] = v;
 }
 
-// Fixed-order sum of the per-block partials (deterministic), one block.
-__global__ void k_finalize(const double* partials, int nblocks, double* result, md_step_record* rec, int* step,
-                           int record) {
-    __shared__ double sh[32];
-    for (int s = 0; s < NPART; ++s) {
-        double v = 0.0;
-        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v += partials[(size_t)b * NPART + s];
-        v = block_sum(v, sh);
-        if (threadIdx.x == 0) result[s] = v;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0 && record) {
-        int k = *step;
-        double myRF = result[3];
-        rec[k].upot = result[0] / 6.0 + result[1] + myRF;
-        rec[k].virial = result[2] + 3.0 * myRF;
-        rec[k].summv2 = result[12];
-        rec[k].sumIw2 = result[15] > 0.0 ? result[13] : 0.0;
-        *step = k + 1;
-    }
+__global__ void k_record(const double* result, md_step_record* rec, int* step) {
+    int k = *step;
+    double myRF = result[3];
+    rec[k].upot = result[0] / 6.0 + result[1] + myRF;
+    rec[k].virial = result[2] + 3.0 * myRF;
+    rec[k].summv2 = result[12];
+    rec[k].sumIw2 = result[15] > 0.0 ? result[13] : 0.0;
+    *step = k + 1;
 }
 
 // ------------------------------------------------------------------ wrap + cells
@@ -354,54 +360,79 @@ __global__ void k_local(State S, float4* xlf, double* rref, const unsigned* need
     rref[3 * i] = S.rx[i]; rref[3 * i + 1] = S.ry[i]; rref[3 * i + 2] = S.rz[i];
 }
 
-// Owner-computes pair-candidate list over the 27 list cells around the home
-// cell (periodic wrap in periodic dimensions).  Candidate test in FP32 local
-// coordinates against (rc + skin)^2 enlarged by a relative 1e-4, so no pair
-// that can come within rc before the next rebuild is missed.
-__global__ void k_build_list(State S, const float4* xl, const int* start, uint32_t* nbr, int* nnb, int maxnb,
-                             int64_t cap, float rl2, unsigned* status, int* need_max, const unsigned* need) {
+// Owner-computes pair-candidate list over the 27 list cells around each
+// molecule's home cell (periodic wrap in periodic dimensions), one warp per
+// home cell: the warp holds up to 32 molecules of the cell in its lanes, walks
+// the 27 neighbour cells 32 candidates at a time (one per lane, coalesced) and
+// appends each molecule's hits with a ballot, so every list row is written
+// contiguously.  Rows are row-major (row i at i * maxnb, maxnb a multiple of
+// 4).  Candidate test in FP32 local coordinates against (rc + skin)^2
+// enlarged by a relative 1e-4, so no pair that can come within rc before the
+// next rebuild is missed.
+__global__ void __launch_bounds__(128) k_build_list(int64_t n, const float4* xl, const int* start, int ncells,
+                                                    uint32_t* nbr, int* nnb, int maxnb, float rl2, unsigned* status,
+                                                    int* need_max, const unsigned* need) {
     if (!*need) return;
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= S.n) return;
-    float4 pi = xl[i];
-    int h = S.home[i];
-    int hc[3] = {h % cP.ln[0], (h / cP.ln[0]) % cP.ln[1], h / (cP.ln[0] * cP.ln[1])};
-    float side[3] = {(float)cP.lside[0], (float)cP.lside[1], (float)cP.lside[2]};
-    int cnt = 0;
-    for (int oz = -1; oz <= 1; ++oz)
-        for (int oy = -1; oy <= 1; ++oy)
-            for (int ox = -1; ox <= 1; ++ox) {
-                int o[3] = {ox, oy, oz};
-                int c[3];
-                bool skip = false;
-                for (int d = 0; d < 3; ++d) {
-                    c[d] = hc[d] + o[d];
-                    if (c[d] < 0 || c[d] >= cP.ln[d]) {
-                        if (!cP.periodic[d]) { skip = true; break; }
-                        c[d] = (c[d] + cP.ln[d]) % cP.ln[d];
+    const int c = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= ncells) return;
+    const int hc[3] = {c % cP.ln[0], (c / cP.ln[0]) % cP.ln[1], c / (cP.ln[0] * cP.ln[1])};
+    const float side[3] = {(float)cP.lside[0], (float)cP.lside[1], (float)cP.lside[2]};
+    const int b = start[c], e = start[c + 1];
+    const unsigned lt = (1u << lane) - 1u;
+    for (int i0 = b; i0 < e; i0 += 32) {
+        const int mi = min(32, e - i0);
+        float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (lane < mi) pi = xl[i0 + lane];
+        int cnt = 0;
+        for (int oz = -1; oz <= 1; ++oz)
+            for (int oy = -1; oy <= 1; ++oy)
+                for (int ox = -1; ox <= 1; ++ox) {
+                    const int o[3] = {ox, oy, oz};
+                    int cc[3];
+                    bool skip = false;
+                    for (int d = 0; d < 3; ++d) {
+                        cc[d] = hc[d] + o[d];
+                        if (cc[d] < 0 || cc[d] >= cP.ln[d]) {
+                            if (!cP.periodic[d]) { skip = true; break; }
+                            cc[d] = (cc[d] + cP.ln[d]) % cP.ln[d];
+                        }
+                    }
+                    if (skip) continue;
+                    const int cell = (cc[2] * cP.ln[1] + cc[1]) * cP.ln[0] + cc[0];
+                    const uint32_t code = (uint32_t)((ox + 1) + 3 * (oy + 1) + 9 * (oz + 1));
+                    const int nb = start[cell], ne = start[cell + 1];
+                    for (int j0 = nb; j0 < ne; j0 += 32) {
+                        const int j = j0 + lane;
+                        const bool valid = j < ne;
+                        float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (valid) pj = xl[j];
+                        // candidate position seen from the home cell's frame
+                        const float qx = pj.x + ox * side[0], qy = pj.y + oy * side[1], qz = pj.z + oz * side[2];
+                        for (int t = 0; t < mi; ++t) {
+                            const float ix = __shfl_sync(0xffffffffu, pi.x, t);
+                            const float iy = __shfl_sync(0xffffffffu, pi.y, t);
+                            const float iz = __shfl_sync(0xffffffffu, pi.z, t);
+                            const float dx = ix - qx, dy = iy - qy, dz = iz - qz;
+                            const float r2 = dx * dx + dy * dy + dz * dz;
+                            const bool hit = valid && r2 < rl2 && j != i0 + t;
+                            const unsigned ball = __ballot_sync(0xffffffffu, hit);
+                            const int ct = __shfl_sync(0xffffffffu, cnt, t);
+                            if (hit) {
+                                const int pos = ct + __popc(ball & lt);
+                                if (pos < maxnb) nbr[(size_t)(i0 + t) * maxnb + pos] = (uint32_t)j | (code << MD_CODE_SHIFT);
+                            }
+                            if (lane == t) cnt += __popc(ball);
+                        }
                     }
                 }
-                if (skip) continue;
-                // with two cells along a periodic axis both offsets reach the same
-                // cell; the far image is removed by the distance test
-                int cell = (c[2] * cP.ln[1] + c[1]) * cP.ln[0] + c[0];
-                uint32_t code = (uint32_t)((ox + 1) + 3 * (oy + 1) + 9 * (oz + 1));
-                float offx = ox * side[0], offy = oy * side[1], offz = oz * side[2];
-                for (int j = start[cell]; j < start[cell + 1]; ++j) {
-                    if (j == i) continue;
-                    float4 pj = xl[j];
-                    float dx = (pi.x - pj.x) - offx, dy = (pi.y - pj.y) - offy, dz = (pi.z - pj.z) - offz;
-                    float r2 = dx * dx + dy * dy + dz * dz;
-                    if (r2 < rl2) {
-                        if (cnt < maxnb) nbr[(int64_t)cnt * cap + i] = (uint32_t)j | (code << MD_CODE_SHIFT);
-                        ++cnt;
-                    }
-                }
+        if (lane < mi) {
+            nnb[i0 + lane] = min(cnt, maxnb);
+            if (cnt > maxnb) {
+                atomicOr(status, ST_LIST_OVERFLOW);
+                atomicMax(need_max, cnt);
             }
-    nnb[i] = min(cnt, maxnb);
-    if (cnt > maxnb) {
-        atomicOr(status, ST_LIST_OVERFLOW);
-        atomicMax(need_max, cnt);
+        }
     }
 }
 
@@ -455,102 +486,156 @@ template <> struct R4<double> { typedef double4 t; };
 // Single-LJ-centre molecules (centre at the molecule origin): the hot path
 // of the 1CLJ benchmarks.  One thread per molecule, list entries streamed
 // column-major.
-template <typename Real>
-__global__ void __launch_bounds__(256) k_force_lj(State S, const float4* xlf, const uint32_t* nbr, const int* nnb,
-                                                  int64_t cap, double* partials) {
-    __shared__ Real soff[27][3];
-    __shared__ double sh[32];
+// Single-LJ-centre molecules (centre at the molecule origin), FP32 pair
+// arithmetic: the hot kernel of the 1CLJ benchmarks.  One thread per
+// molecule streams its candidate row four entries per 16-byte load, gathers
+// the four neighbour positions before computing (latency hiding), re-decides
+// pairs within 4e-6 relative of a cut-off in FP64, and accumulates F with
+// Kahan compensation; Vi, Upot and virial are plain FP32 per molecule and
+// FP64 across molecules.
+__global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __restrict__ xlf,
+                                                       const uint32_t* __restrict__ nbr, const int* __restrict__ nnb,
+                                                       int maxnb, double* partials, int pstride) {
+    __shared__ float soff[27][3];
     if (threadIdx.x < 27) {
         int t = threadIdx.x;
-        soff[t][0] = (Real)((t % 3 - 1) * cP.lside[0]);
-        soff[t][1] = (Real)(((t / 3) % 3 - 1) * cP.lside[1]);
-        soff[t][2] = (Real)((t / 9 - 1) * cP.lside[2]);
+        soff[t][0] = (float)((t % 3 - 1) * cP.lside[0]);
+        soff[t][1] = (float)(((t / 3) % 3 - 1) * cP.lside[1]);
+        soff[t][2] = (float)((t / 9 - 1) * cP.lside[2]);
     }
     __syncthreads();
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    typename Acc<Real>::type fx, fy, fz, vx, vy, vz, up, vir;
-    fx.init(); fy.init(); fz.init(); vx.init(); vy.init(); vz.init(); up.init(); vir.init();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    KSum fx, fy, fz;
+    fx.init(); fy.init(); fz.init();
+    float vx = 0.f, vy = 0.f, vz = 0.f, up = 0.f, vir = 0.f;
     int npairs = 0, nmol = 0;
     if (i < S.n) {
-        float4 p4 = xlf[i];
+        const float4 p4 = xlf[i];
         const int ci = __float_as_int(p4.w);
         const int gi = cP.comp[ci].ljoff;
-        Real pix, piy, piz;
-        if (sizeof(Real) == 4) {
-            pix = p4.x; piy = p4.y; piz = p4.z;
-        } else {
-            pix = S.rx[i]; piy = S.ry[i]; piz = S.rz[i];
-        }
         const int cnt = nnb[i];
-        const Real rclj2 = sizeof(Real) == 4 ? (Real)cP.rclj2f : (Real)cP.rclj2;
-        const Real rc2 = sizeof(Real) == 4 ? (Real)cP.rc2f : (Real)cP.rc2;
-        const bool one_comp = cP.ncomp == 1;
-        Real e24 = (Real)cP.eps24[gi * cP.nlj + gi], s2 = (Real)cP.sig2[gi * cP.nlj + gi];
-        Real sh6 = (Real)cP.shift6[gi * cP.nlj + gi];
+        const float rclj2 = cP.rclj2f, rc2 = cP.rc2f;
+        const float bl_lo = cP.band_lo_lj, bl_hi = cP.band_hi_lj, be_lo = cP.band_lo, be_hi = cP.band_hi;
+        const bool one_comp = cP.ncomp == 1, same_cut = cP.rc2 == cP.rclj2;
+        float e24 = (float)cP.eps24[gi * cP.nlj + gi], s2 = (float)cP.sig2[gi * cP.nlj + gi];
+        float sh6 = (float)cP.shift6[gi * cP.nlj + gi];
         int cur = gi;
-        for (int k = 0; k < cnt; ++k) {
-            uint32_t e = __ldg(&nbr[(int64_t)k * cap + i]);
-            int64_t j = e & MD_INDEX_MASK;
-            uint32_t code = e >> MD_CODE_SHIFT;
-            float4 pj = __ldg(&xlf[j]);
-            Real dx, dy, dz;
-            if (sizeof(Real) == 4) {
-                dx = (pix - (Real)pj.x) - soff[code][0];
-                dy = (piy - (Real)pj.y) - soff[code][1];
-                dz = (piz - (Real)pj.z) - soff[code][2];
-            } else {
-                double shf[3];
-                image_shift(S.home[i], code, shf);
-                dx = pix - (S.rx[j] + shf[0]);
-                dy = piy - (S.ry[j] + shf[1]);
-                dz = piz - (S.rz[j] + shf[2]);
-            }
-            Real r2 = dx * dx + (dy * dy + dz * dz);
-            bool in = r2 < rclj2, in_rc = r2 < rc2;
-            if (sizeof(Real) == 4) {
-                bool bl = r2 > (Real)cP.band_lo_lj && r2 < (Real)cP.band_hi_lj;
-                bool be = r2 > (Real)cP.band_lo && r2 < (Real)cP.band_hi;
-                if (bl || be) {
-                    double r2d = fp64_r2(S, i, j, code);
-                    if (bl) in = r2d < cP.rclj2;
-                    if (be) in_rc = r2d < cP.rc2;
+        const uint4* row = reinterpret_cast<const uint4*>(nbr + (size_t)i * maxnb);
+        for (int k = 0; k < cnt; k += 4) {
+            const uint4 e4 = __ldg(row + (k >> 2));
+            const uint32_t ee[4] = {e4.x, e4.y, e4.z, e4.w};
+            float4 pj[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) pj[t] = __ldg(&xlf[(k + t < cnt) ? (ee[t] & MD_INDEX_MASK) : i]);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                if (k + t >= cnt) break;
+                const int j = (int)(ee[t] & MD_INDEX_MASK);
+                const uint32_t code = ee[t] >> MD_CODE_SHIFT;
+                const float dx = (p4.x - pj[t].x) - soff[code][0];
+                const float dy = (p4.y - pj[t].y) - soff[code][1];
+                const float dz = (p4.z - pj[t].z) - soff[code][2];
+                const float r2 = dx * dx + (dy * dy + dz * dz);
+                bool in = r2 < rclj2, in_rc = same_cut ? in : r2 < rc2;
+                if ((r2 > bl_lo && r2 < bl_hi) || (r2 > be_lo && r2 < be_hi)) {
+                    const double r2d = fp64_r2(S, i, j, code);
+                    in = r2d < cP.rclj2;
+                    in_rc = r2d < cP.rc2;
                 }
-            }
-            const bool macro = j > i;
-            nmol += (in_rc && macro) ? 1 : 0;
-            if (!in) continue;
-            if (!one_comp) {
-                const int gj = cP.comp[__float_as_int(pj.w)].ljoff;
-                if (gj != cur) {
-                    cur = gj;
-                    e24 = (Real)cP.eps24[gi * cP.nlj + gj];
-                    s2 = (Real)cP.sig2[gi * cP.nlj + gj];
-                    sh6 = (Real)cP.shift6[gi * cP.nlj + gj];
+                const bool macro = j > i;
+                nmol += (in_rc && macro) ? 1 : 0;
+                if (!in) continue;
+                if (!one_comp) {
+                    const int gj = cP.comp[__float_as_int(pj[t].w)].ljoff;
+                    if (gj != cur) {
+                        cur = gj;
+                        e24 = (float)cP.eps24[gi * cP.nlj + gj];
+                        s2 = (float)cP.sig2[gi * cP.nlj + gj];
+                        sh6 = (float)cP.shift6[gi * cP.nlj + gj];
+                    }
                 }
-            }
-            Real f[3], V[3], u;
-            const Real d[3] = {dx, dy, dz};
-            lj_pair<Real>(d, d, r2, e24, s2, sh6, f, V, u);
-            fx.add(f[0]); fy.add(f[1]); fz.add(f[2]);
-            vx.add(V[0]); vy.add(V[1]); vz.add(V[2]);
-            if (macro) {
-                up.add(u);
-                vir.add(V[0] + V[1] + V[2]);
-                ++npairs;
+                // VCP::_loopBodyLJ: scale = eps24 / r^2 (2 lj12 - lj6)
+                const float r2inv = __fdividef(1.0f, r2);
+                const float lj2 = s2 * r2inv;
+                const float lj6 = lj2 * lj2 * lj2;
+                const float lj12m6 = lj6 * lj6 - lj6;
+                const float scale = e24 * r2inv * (lj6 * lj6 + lj12m6);
+                const float f0 = dx * scale, f1 = dy * scale, f2 = dz * scale;
+                fx.add(f0); fy.add(f1); fz.add(f2);
+                const float V0 = dx * f0, V1 = dy * f1, V2 = dz * f2;
+                vx += V0; vy += V1; vz += V2;
+                if (macro) {
+                    up += e24 * lj12m6 + sh6;
+                    vir += V0 + V1 + V2;
+                    ++npairs;
+                }
             }
         }
         S.Fx[i] = fx.value(); S.Fy[i] = fy.value(); S.Fz[i] = fz.value();
         S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
-        S.Vx[i] = 0.5 * vx.value(); S.Vy[i] = 0.5 * vy.value(); S.Vz[i] = 0.5 * vz.value();
+        S.Vx[i] = 0.5 * (double)vx; S.Vy[i] = 0.5 * (double)vy; S.Vz[i] = 0.5 * (double)vz;
     }
-    double* P = partials + (size_t)blockIdx.x * NPART;
-    double t;
-    t = block_sum(up.value(), sh); if (threadIdx.x == 0) P[0] = t;
-    t = block_sum(vir.value(), sh); if (threadIdx.x == 0) P[2] = t;
-    t = block_sum((double)npairs, sh);
-    if (threadIdx.x == 0) { P[1] = 0.0; P[3] = 0.0; P[5] = t; for (int s = 6; s < 12; ++s) P[s] = 0.0; }
-    t = block_sum((double)nmol, sh);
-    if (threadIdx.x == 0) P[4] = t;
+    warp_partial(partials, pstride, 0, (double)up);
+    warp_partial(partials, pstride, 1, 0.0);
+    warp_partial(partials, pstride, 2, (double)vir);
+    warp_partial(partials, pstride, 3, 0.0);
+    warp_partial(partials, pstride, 4, (double)nmol);
+    warp_partial(partials, pstride, 5, (double)npairs);
+    for (int sl = 6; sl < 12; ++sl) warp_partial(partials, pstride, sl, 0.0);
+}
+
+// FP64 variant: absolute FP64 positions with the reference's halo image
+// shift r_j +- L, FP64 arithmetic and accumulation throughout.
+__global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __restrict__ xlf,
+                                                    const uint32_t* __restrict__ nbr, const int* __restrict__ nnb,
+                                                    int maxnb, double* partials, int pstride) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double fx = 0, fy = 0, fz = 0, vx = 0, vy = 0, vz = 0, up = 0, vir = 0;
+    int npairs = 0, nmol = 0;
+    if (i < S.n) {
+        const int ci = S.comp[i];
+        const int gi = cP.comp[ci].ljoff;
+        const double pix = S.rx[i], piy = S.ry[i], piz = S.rz[i];
+        const int h = S.home[i];
+        const int cnt = nnb[i];
+        const uint32_t* row = nbr + (size_t)i * maxnb;
+        for (int k = 0; k < cnt; ++k) {
+            const uint32_t e = __ldg(row + k);
+            const int j = (int)(e & MD_INDEX_MASK);
+            const uint32_t code = e >> MD_CODE_SHIFT;
+            double shf[3];
+            image_shift(h, code, shf);
+            const double dx = pix - (S.rx[j] + shf[0]);
+            const double dy = piy - (S.ry[j] + shf[1]);
+            const double dz = piz - (S.rz[j] + shf[2]);
+            const double r2 = dx * dx + (dy * dy + dz * dz);
+            const bool macro = j > i;
+            nmol += (r2 < cP.rc2 && macro) ? 1 : 0;
+            if (!(r2 < cP.rclj2)) continue;
+            const int gj = cP.comp[S.comp[j]].ljoff;
+            double f[3], V[3], u;
+            const double d[3] = {dx, dy, dz};
+            lj_pair<double>(d, d, r2, cP.eps24[gi * cP.nlj + gj], cP.sig2[gi * cP.nlj + gj], cP.shift6[gi * cP.nlj + gj],
+                            f, V, u);
+            fx += f[0]; fy += f[1]; fz += f[2];
+            vx += V[0]; vy += V[1]; vz += V[2];
+            if (macro) {
+                up += u;
+                vir += V[0] + V[1] + V[2];
+                ++npairs;
+            }
+        }
+        S.Fx[i] = fx; S.Fy[i] = fy; S.Fz[i] = fz;
+        S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
+        S.Vx[i] = 0.5 * vx; S.Vy[i] = 0.5 * vy; S.Vz[i] = 0.5 * vz;
+    }
+    warp_partial(partials, pstride, 0, up);
+    warp_partial(partials, pstride, 1, 0.0);
+    warp_partial(partials, pstride, 2, vir);
+    warp_partial(partials, pstride, 3, 0.0);
+    warp_partial(partials, pstride, 4, (double)nmol);
+    warp_partial(partials, pstride, 5, (double)npairs);
+    for (int sl = 6; sl < 12; ++sl) warp_partial(partials, pstride, sl, 0.0);
 }
 
 // General multi-site molecules: all site pairs of every molecule pair inside
@@ -559,10 +644,9 @@ __global__ void __launch_bounds__(256) k_force_lj(State S, const float4* xlf, co
 // Vi = 1/2 sum m_d o f.
 template <typename Real>
 __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, const Real* sd, const Real* se,
-                                                  int stride, const uint32_t* nbr, const int* nnb, int64_t cap,
-                                                  double* partials) {
+                                                  int stride, const uint32_t* nbr, const int* nnb, int maxnb,
+                                                  double* partials, int pstride) {
     __shared__ Real soff[27][3];
-    __shared__ double sh[32];
     if (threadIdx.x < 27) {
         int t = threadIdx.x;
         soff[t][0] = (Real)((t % 3 - 1) * cP.lside[0]);
@@ -590,7 +674,7 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
         const Real rc2 = sizeof(Real) == 4 ? (Real)cP.rc2f : (Real)cP.rc2;
         const Real epsRF = (Real)cP.epsRFInvrc3;
         for (int k = 0; k < cnt; ++k) {
-            uint32_t e = __ldg(&nbr[(int64_t)k * cap + i]);
+            uint32_t e = __ldg(&nbr[(size_t)i * maxnb + k]);
             int64_t j = e & MD_INDEX_MASK;
             uint32_t code = e >> MD_CODE_SHIFT;
             Real md[3];
@@ -671,16 +755,11 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
         S.Mx[i] = M[0].value(); S.My[i] = M[1].value(); S.Mz[i] = M[2].value();
         S.Vx[i] = 0.5 * V[0].value(); S.Vy[i] = 0.5 * V[1].value(); S.Vz[i] = 0.5 * V[2].value();
     }
-    double* P = partials + (size_t)blockIdx.x * NPART;
-    double t;
-    t = block_sum(u6.value(), sh); if (threadIdx.x == 0) P[0] = t;
-    t = block_sum(ux.value(), sh); if (threadIdx.x == 0) P[1] = t;
-    t = block_sum(vir.value(), sh); if (threadIdx.x == 0) P[2] = t;
-    t = block_sum(-rf.value(), sh); if (threadIdx.x == 0) P[3] = t;
-    for (int s = 0; s < 8; ++s) {
-        t = block_sum((double)cnt_pairs[s], sh);
-        if (threadIdx.x == 0) P[4 + s] = t;
-    }
+    warp_partial(partials, pstride, 0, u6.value());
+    warp_partial(partials, pstride, 1, ux.value());
+    warp_partial(partials, pstride, 2, vir.value());
+    warp_partial(partials, pstride, 3, -rf.value());
+    for (int sl = 0; sl < 8; ++sl) warp_partial(partials, pstride, 4 + sl, (double)cnt_pairs[sl]);
 }
 
 // ------------------------------------------------------------------ integration
@@ -762,8 +841,7 @@ __global__ void k_sum_int(const int* a, int64_t n, unsigned long long* out) {
 }
 
 // FullMolecule::upd_postF with the Leapfrog sums.
-__global__ void k_post(State S, double dt, double* partials) {
-    __shared__ double sh[32];
+__global__ void k_post(State S, double dt, double* partials, int pstride) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double mv2 = 0.0, iw2 = 0.0, rot = 0.0, one = 0.0;
     if (i < S.n) {
@@ -794,12 +872,10 @@ __global__ void k_post(State S, double dt, double* partials) {
         rot = C.rot_dof;
         one = 1.0;
     }
-    double* P = partials + (size_t)blockIdx.x * NPART;
-    double t;
-    t = block_sum(mv2, sh); if (threadIdx.x == 0) P[12] = t;
-    t = block_sum(iw2, sh); if (threadIdx.x == 0) P[13] = t;
-    t = block_sum(one, sh); if (threadIdx.x == 0) P[14] = t;
-    t = block_sum(rot, sh); if (threadIdx.x == 0) P[15] = t;
+    warp_partial(partials, pstride, 12, mv2);
+    warp_partial(partials, pstride, 13, iw2);
+    warp_partial(partials, pstride, 14, one);
+    warp_partial(partials, pstride, 15, rot);
 }
 
 #include "md_adjoint.inc"
