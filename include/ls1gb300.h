@@ -169,6 +169,29 @@ int md_run(md_ctx* ctx, double dt, int32_t nsteps, md_step_record* rec);
 int md_adjoint(md_ctx* ctx, double gU, double gW, const double* gF, double* grad_r, double* grad_params,
                int32_t nparam);
 
+/* ---- allocation-free force evaluation (no counterpart in the reference)
+ * For callers that cannot allocate device memory: code recording into a CUDA
+ * graph owned by a larger application, programs whose device memory comes
+ * from their own pool, real-time drivers that forbid allocation after
+ * start-up.  Computes, for a periodic box [0, box) of single-centre LJ
+ * molecules (one component, centre at the molecule origin), the FP64 forces
+ * d_F (n x 3, device), and d_upot_virial[0] = Upot, [1] = virial (device), as
+ * md_compute_forces does, from device positions d_r (n x 3), on `stream`
+ * (NULL: the default stream).  It allocates nothing: its scratch is one
+ * file-scope device array of MD_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * the library keeps until exit.  Limits: n <= MD_NOALLOC_MAX_N, at least
+ * three cells of edge >= rc per axis and at most MD_NOALLOC_MAX_CELLS cells;
+ * larger problems return MD_ERR_CAPACITY, too few cells MD_ERR_UNSUPPORTED.
+ * The first call on a device (with that device current) looks up the scratch
+ * address and should come before any stream capture.  All calls share the
+ * scratch, which keeps the previous call's contents: calls that overlap on
+ * the GPU race and must be serialised by the caller. */
+#define MD_NOALLOC_MAX_N 131072
+#define MD_NOALLOC_MAX_CELLS 65536
+#define MD_NOALLOC_SCRATCH_BYTES 1966080
+int md_forces_lj_noalloc(const double* d_r, int64_t n, const double box[3], double rc, double eps, double sigma,
+                         double shift6, double* d_F, double* d_upot_virial, void* stream);
+
 /* Wait for all work of the context. */
 int md_sync(md_ctx* ctx);
 
