@@ -88,25 +88,38 @@ __device__ double block_sum(double v, double* sh) {
     return r;
 }
 
-// slots 0..11 come from the force kernel (nw_force warps), 12..15 from the
+// slots 0..11 come from the force kernel (nw_force warps), 12..13 from the
 // post-force half step (nw_post warps); a count of 0 leaves a slot at 0.
-__global__ void k_finalize(const double* partials, int pstride, int nw_force, int nw_post, double* result) {
+// Stage 1: FIN_SEG blocks per slot each sum a contiguous segment; stage 2
+// sums the FIN_SEG segment sums of each slot in order (deterministic).
+#define FIN_SEG 64
+__global__ void k_finalize1(const double* partials, int pstride, int nw_force, int nw_post, int nw_rot, double* seg) {
     __shared__ double sh[32];
-    const int s = blockIdx.x;
-    const int nw = s < 12 ? nw_force : nw_post;
+    const int s = blockIdx.y, b = blockIdx.x;
+    const int nw = s < 12 ? nw_force : (s == 12 ? nw_post : (s == 13 ? nw_rot : 0));
+    const int per = (nw + FIN_SEG - 1) / FIN_SEG;
+    const int lo = b * per, hi = min(nw, lo + per);
     double v = 0.0;
-    for (int b = threadIdx.x; b < nw; b += blockDim.x) v += partials[(size_t)s * pstride + b];
+    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) v += partials[(size_t)s * pstride + k];
     v = block_sum(v, sh);
-    if (threadIdx.x == 0) result[s] = v;
+    if (threadIdx.x == 0) seg[s * FIN_SEG + b] = v;
 }
 
-__global__ void k_record(const double* result, md_step_record* rec, int* step) {
+__global__ void k_finalize2(const double* seg, double* result) {
+    const int s = threadIdx.x;
+    if (s >= NPART) return;
+    double v = 0.0;
+    for (int b = 0; b < FIN_SEG; ++b) v += seg[s * FIN_SEG + b];
+    result[s] = v;
+}
+
+__global__ void k_record(const double* result, md_step_record* rec, int* step, int has_rot_dof) {
     int k = *step;
     double myRF = result[3];
     rec[k].upot = result[0] / 6.0 + result[1] + myRF;
     rec[k].virial = result[2] + 3.0 * myRF;
     rec[k].summv2 = result[12];
-    rec[k].sumIw2 = result[15] > 0.0 ? result[13] : 0.0;
+    rec[k].sumIw2 = has_rot_dof ? result[13] : 0.0;
     *step = k + 1;
 }
 
@@ -119,10 +132,7 @@ __device__ __forceinline__ double& coord(State& S, int d, int64_t i) {
 // lower face first (shift +L, clamp below max), then upper face (shift -L,
 // clamp to min).  Molecules further than rc outside the box are lost in the
 // reference; they raise ST_LOST here.
-__global__ void k_wrap(State S, unsigned* status, unsigned long long* nwrapped, const unsigned* need) {
-    if (need && !*need) return;
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= S.n) return;
+__device__ void wrap_molecule(State& S, int64_t i, unsigned* status, unsigned long long* nwrapped) {
     double r[3] = {S.rx[i], S.ry[i], S.rz[i]};
     int moved = 0;
     for (int d = 0; d < 3; ++d) {
@@ -157,6 +167,13 @@ __global__ void k_wrap(State S, unsigned* status, unsigned long long* nwrapped, 
         S.rx[i] = r[0]; S.ry[i] = r[1]; S.rz[i] = r[2];
         atomicAdd(nwrapped, 1ull);
     }
+}
+
+__global__ void k_wrap(State S, unsigned* status, unsigned long long* nwrapped, const unsigned* need) {
+    if (need && !*need) return;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    wrap_molecule(S, i, status, nwrapped);
 }
 
 // LinkedCells::getCellIndexOfPoint with the border table of
@@ -246,24 +263,49 @@ __device__ __forceinline__ int list_cell_coord(double x, int d) {
     return max(0, min(c, cP.ln[d] - 1));
 }
 
-__global__ void k_list_hist(State S, int* mcell, int* counts, const unsigned* need) {
+__device__ void wrap_molecule(State& S, int64_t i, unsigned* status, unsigned long long* nwrapped);
+
+// Leaving-particle wrap for molecules outside the box, then the list cell of
+// every molecule and its histogram.
+__global__ void k_list_hist(State S, int* mcell, int* counts, unsigned* status, unsigned long long* nwrapped,
+                            const unsigned* need) {
     if (!*need) return;
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= S.n) return;
+    const double x = S.rx[i], y = S.ry[i], z = S.rz[i];
+    if (!(x >= cP.bmin[0] && x < cP.bmax[0] && y >= cP.bmin[1] && y < cP.bmax[1] && z >= cP.bmin[2] && z < cP.bmax[2]))
+        wrap_molecule(S, i, status, nwrapped);
     int cx = list_cell_coord(S.rx[i], 0), cy = list_cell_coord(S.ry[i], 1), cz = list_cell_coord(S.rz[i], 2);
     int c = (cz * cP.ln[1] + cy) * cP.ln[0] + cx;
     mcell[i] = c;
     atomicAdd(&counts[c], 1);
 }
 
-// Exclusive scan of counts[0..n) into start[0..n], one block of 1024 threads.
-__global__ void k_scan(const int* counts, int* start, int n, int* cursor, const unsigned* need) {
+// Exclusive scan of counts[0..n) into start[0..n] (and cursor) in three
+// passes: per-block sums, one block scanning the block sums, per-block scans.
+#define SCAN_BLOCK 1024
+__global__ void k_scan1(const int* counts, int n, int* bsum, const unsigned* need) {
+    if (!*need) return;
+    __shared__ int sh[32];
+    int i = blockIdx.x * SCAN_BLOCK + threadIdx.x;
+    int v = i < n ? counts[i] : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = sh[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) bsum[blockIdx.x] = v;
+    }
+}
+
+__global__ void k_scan2(int* bsum, int nb, int* total_out, const unsigned* need) {
     if (!*need) return;
     __shared__ int sh[1024];
-    int per = (n + blockDim.x - 1) / blockDim.x;
-    int b = threadIdx.x * per, e = min(n, b + per);
+    int per = (nb + blockDim.x - 1) / blockDim.x;
+    int b = threadIdx.x * per, e = min(nb, b + per);
     int s = 0;
-    for (int k = b; k < e; ++k) s += counts[k];
+    for (int k = b; k < e; ++k) s += bsum[k];
     sh[threadIdx.x] = s;
     __syncthreads();
     for (int off = 1; off < blockDim.x; off <<= 1) {
@@ -274,11 +316,40 @@ __global__ void k_scan(const int* counts, int* start, int n, int* cursor, const 
     }
     int run = sh[threadIdx.x] - s;
     for (int k = b; k < e; ++k) {
-        start[k] = run;
-        cursor[k] = run;
-        run += counts[k];
+        int c = bsum[k];
+        bsum[k] = run;
+        run += c;
     }
-    if (threadIdx.x == blockDim.x - 1) start[n] = sh[threadIdx.x];
+    if (threadIdx.x == blockDim.x - 1) *total_out = sh[threadIdx.x];
+}
+
+__global__ void k_scan3(const int* counts, int n, const int* boff, int* start, int* cursor, const unsigned* need) {
+    if (!*need) return;
+    __shared__ int sh[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int i = blockIdx.x * SCAN_BLOCK + threadIdx.x;
+    int v = i < n ? counts[i] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int t = sh[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        sh[lane] = t;
+    }
+    __syncthreads();
+    int excl = boff[blockIdx.x] + (w > 0 ? sh[w - 1] : 0) + x - v;
+    if (i < n) {
+        start[i] = excl;
+        cursor[i] = excl;
+    }
 }
 
 __global__ void k_list_scatter(int64_t n, const int* mcell, int* cursor, int* perm, const unsigned* need) {
@@ -337,54 +408,62 @@ __global__ void k_permute(State dst, State src, const int* perm, const int* mcel
     dst.home[k] = mcell[i];
 }
 
-// Local coordinates relative to the home-cell origin (and a copy of the
-// reference positions for the displacement test).
-template <typename Real4>
-__device__ __forceinline__ void make_local(const State& S, int64_t i, Real4* xl) {
-    int h = S.home[i];
-    int cx = h % cP.ln[0], cy = (h / cP.ln[0]) % cP.ln[1], cz = h / (cP.ln[0] * cP.ln[1]);
-    double ox = cP.bmin[0] + cx * cP.lside[0], oy = cP.bmin[1] + cy * cP.lside[1], oz = cP.bmin[2] + cz * cP.lside[2];
-    Real4 p;
-    p.x = S.rx[i] - ox;
-    p.y = S.ry[i] - oy;
-    p.z = S.rz[i] - oz;
-    p.w = __int_as_float(S.comp[i]);
-    xl[i] = p;
-}
-
-__global__ void k_local(State S, float4* xlf, double* rref, const unsigned* need) {
+// Local coordinates relative to the home-cell origin.  At a list rebuild the
+// origin (FP64) and the local coordinates then (FP32, for the displacement
+// test) are stored per molecule; every pre-force step recomputes the local
+// coordinates from the FP64 position.
+__global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, const unsigned* need) {
     if (need && !*need) return;
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= S.n) return;
-    make_local<float4>(S, i, xlf);
-    rref[3 * i] = S.rx[i]; rref[3 * i + 1] = S.ry[i]; rref[3 * i + 2] = S.rz[i];
+    int h = S.home[i];
+    int cx = h % cP.ln[0], cy = (h / cP.ln[0]) % cP.ln[1], cz = h / (cP.ln[0] * cP.ln[1]);
+    double ox = cP.bmin[0] + cx * cP.lside[0], oy = cP.bmin[1] + cy * cP.lside[1], oz = cP.bmin[2] + cz * cP.lside[2];
+    origin[3 * i] = ox; origin[3 * i + 1] = oy; origin[3 * i + 2] = oz;
+    float4 p;
+    p.x = (float)(S.rx[i] - ox);
+    p.y = (float)(S.ry[i] - oy);
+    p.z = (float)(S.rz[i] - oz);
+    p.w = __int_as_float(S.comp[i]);
+    xlf[i] = p;
+    xlref[i] = p;
 }
 
 // Owner-computes pair-candidate list over the 27 list cells around each
-// molecule's home cell (periodic wrap in periodic dimensions), one warp per
-// home cell: the warp holds up to 32 molecules of the cell in its lanes, walks
-// the 27 neighbour cells 32 candidates at a time (one per lane, coalesced) and
-// appends each molecule's hits with a ballot, so every list row is written
-// contiguously.  Rows are row-major (row i at i * maxnb, maxnb a multiple of
-// 4).  Candidate test in FP32 local coordinates against (rc + skin)^2
-// enlarged by a relative 1e-4, so no pair that can come within rc before the
-// next rebuild is missed.
-__global__ void __launch_bounds__(128) k_build_list(int64_t n, const float4* xl, const int* start, int ncells,
-                                                    uint32_t* nbr, int* nnb, int maxnb, float rl2, unsigned* status,
-                                                    int* need_max, const unsigned* need) {
+// molecule's home cell (periodic wrap in periodic dimensions).  One warp per
+// home cell holds up to 32 of its molecules, one per lane.  For each
+// neighbour cell the warp stages 32 candidates at a time in shared memory
+// (coalesced load, already shifted into the home cell's frame); every lane
+// tests its molecule against the staged candidates (broadcast reads) and
+// appends hits to its own 8-entry shared-memory buffer, flushed as two
+// 16-byte stores into its row.  Rows are row-major (row i at i * maxnb,
+// maxnb a multiple of 4).  Candidate test in FP32 local coordinates against
+// (rc + skin)^2 enlarged by a relative 2e-4, so no pair that can come within
+// rc before the next rebuild is missed.
+#define BL_WARPS 4
+#define BL_BUF 8
+__global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const float4* xl, const int* start,
+                                                              int ncells, uint32_t* nbr, int* nnb, int maxnb,
+                                                              float rl2, unsigned* status, int* need_max,
+                                                              const unsigned* need) {
     if (!*need) return;
-    const int c = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (c >= ncells) return;
+    __shared__ float4 scand[BL_WARPS][32];
+    __shared__ uint32_t sent[BL_WARPS][32];
+    __shared__ uint32_t sbuf[BL_WARPS][32][BL_BUF + 1];  // +1: no bank conflicts between lanes
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * BL_WARPS + wl;
+    if (c >= ncells) return;  // warp-uniform; only warp-level synchronisation below
     const int hc[3] = {c % cP.ln[0], (c / cP.ln[0]) % cP.ln[1], c / (cP.ln[0] * cP.ln[1])};
     const float side[3] = {(float)cP.lside[0], (float)cP.lside[1], (float)cP.lside[2]};
     const int b = start[c], e = start[c + 1];
-    const unsigned lt = (1u << lane) - 1u;
+    uint32_t* buf = sbuf[wl][lane];
     for (int i0 = b; i0 < e; i0 += 32) {
-        const int mi = min(32, e - i0);
+        const int i = i0 + lane;
+        const bool own = i < e;
         float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (lane < mi) pi = xl[i0 + lane];
-        int cnt = 0;
+        if (own) pi = xl[i];
+        int cnt = 0, nb = 0;
+        uint32_t* row = nbr + (size_t)(own ? i : 0) * maxnb;
         for (int oz = -1; oz <= 1; ++oz)
             for (int oy = -1; oy <= 1; ++oy)
                 for (int ox = -1; ox <= 1; ++ox) {
@@ -401,33 +480,43 @@ __global__ void __launch_bounds__(128) k_build_list(int64_t n, const float4* xl,
                     if (skip) continue;
                     const int cell = (cc[2] * cP.ln[1] + cc[1]) * cP.ln[0] + cc[0];
                     const uint32_t code = (uint32_t)((ox + 1) + 3 * (oy + 1) + 9 * (oz + 1));
-                    const int nb = start[cell], ne = start[cell + 1];
-                    for (int j0 = nb; j0 < ne; j0 += 32) {
-                        const int j = j0 + lane;
-                        const bool valid = j < ne;
-                        float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (valid) pj = xl[j];
-                        // candidate position seen from the home cell's frame
-                        const float qx = pj.x + ox * side[0], qy = pj.y + oy * side[1], qz = pj.z + oz * side[2];
-                        for (int t = 0; t < mi; ++t) {
-                            const float ix = __shfl_sync(0xffffffffu, pi.x, t);
-                            const float iy = __shfl_sync(0xffffffffu, pi.y, t);
-                            const float iz = __shfl_sync(0xffffffffu, pi.z, t);
-                            const float dx = ix - qx, dy = iy - qy, dz = iz - qz;
+                    const float sx = ox * side[0], sy = oy * side[1], sz = oz * side[2];
+                    const int nb0 = start[cell], ne = start[cell + 1];
+                    for (int j0 = nb0; j0 < ne; j0 += 32) {
+                        const int m = min(32, ne - j0);
+                        __syncwarp();
+                        if (lane < m) {
+                            const float4 pj = xl[j0 + lane];
+                            scand[wl][lane] = make_float4(pj.x + sx, pj.y + sy, pj.z + sz, 0.f);
+                            sent[wl][lane] = (uint32_t)(j0 + lane) | (code << MD_CODE_SHIFT);
+                        }
+                        __syncwarp();
+                        if (!own) continue;
+                        for (int t = 0; t < m; ++t) {
+                            const float4 q = scand[wl][t];
+                            const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
                             const float r2 = dx * dx + dy * dy + dz * dz;
-                            const bool hit = valid && r2 < rl2 && j != i0 + t;
-                            const unsigned ball = __ballot_sync(0xffffffffu, hit);
-                            const int ct = __shfl_sync(0xffffffffu, cnt, t);
-                            if (hit) {
-                                const int pos = ct + __popc(ball & lt);
-                                if (pos < maxnb) nbr[(size_t)(i0 + t) * maxnb + pos] = (uint32_t)j | (code << MD_CODE_SHIFT);
+                            if (r2 < rl2 && j0 + t != i) {
+                                buf[nb++] = sent[wl][t];
+                                if (nb == BL_BUF) {
+                                    if (cnt + BL_BUF <= maxnb) {
+                                        uint4* dst = reinterpret_cast<uint4*>(row + cnt);
+                                        dst[0] = make_uint4(buf[0], buf[1], buf[2], buf[3]);
+                                        dst[1] = make_uint4(buf[4], buf[5], buf[6], buf[7]);
+                                    } else {
+                                        for (int u = 0; u < BL_BUF && cnt + u < maxnb; ++u) row[cnt + u] = buf[u];
+                                    }
+                                    cnt += BL_BUF;
+                                    nb = 0;
+                                }
                             }
-                            if (lane == t) cnt += __popc(ball);
                         }
                     }
                 }
-        if (lane < mi) {
-            nnb[i0 + lane] = min(cnt, maxnb);
+        if (own) {
+            for (int u = 0; u < nb && cnt + u < maxnb; ++u) row[cnt + u] = buf[u];
+            cnt += nb;
+            nnb[i] = min(cnt, maxnb);
             if (cnt > maxnb) {
                 atomicOr(status, ST_LIST_OVERFLOW);
                 atomicMax(need_max, cnt);
@@ -496,12 +585,11 @@ template <> struct R4<double> { typedef double4 t; };
 __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __restrict__ xlf,
                                                        const uint32_t* __restrict__ nbr, const int* __restrict__ nnb,
                                                        int maxnb, double* partials, int pstride) {
-    __shared__ float soff[27][3];
+    __shared__ float4 soff[27];
     if (threadIdx.x < 27) {
         int t = threadIdx.x;
-        soff[t][0] = (float)((t % 3 - 1) * cP.lside[0]);
-        soff[t][1] = (float)(((t / 3) % 3 - 1) * cP.lside[1]);
-        soff[t][2] = (float)((t / 9 - 1) * cP.lside[2]);
+        soff[t] = make_float4((float)((t % 3 - 1) * cP.lside[0]), (float)(((t / 3) % 3 - 1) * cP.lside[1]),
+                              (float)((t / 9 - 1) * cP.lside[2]), 0.f);
     }
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -515,7 +603,7 @@ __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __
         const int gi = cP.comp[ci].ljoff;
         const int cnt = nnb[i];
         const float rclj2 = cP.rclj2f, rc2 = cP.rc2f;
-        const float bl_lo = cP.band_lo_lj, bl_hi = cP.band_hi_lj, be_lo = cP.band_lo, be_hi = cP.band_hi;
+        const float band_lj = cP.band_hi_lj - cP.rclj2f, band_rc = cP.band_hi - cP.rc2f;
         const bool one_comp = cP.ncomp == 1, same_cut = cP.rc2 == cP.rclj2;
         float e24 = (float)cP.eps24[gi * cP.nlj + gi], s2 = (float)cP.sig2[gi * cP.nlj + gi];
         float sh6 = (float)cP.shift6[gi * cP.nlj + gi];
@@ -527,23 +615,29 @@ __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __
             float4 pj[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) pj[t] = __ldg(&xlf[(k + t < cnt) ? (ee[t] & MD_INDEX_MASK) : i]);
+            float gx = 0.f, gy = 0.f, gz = 0.f;  // this group's force, added compensated below
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
                 if (k + t >= cnt) break;
                 const int j = (int)(ee[t] & MD_INDEX_MASK);
-                const uint32_t code = ee[t] >> MD_CODE_SHIFT;
-                const float dx = (p4.x - pj[t].x) - soff[code][0];
-                const float dy = (p4.y - pj[t].y) - soff[code][1];
-                const float dz = (p4.z - pj[t].z) - soff[code][2];
+                const float4 o = soff[ee[t] >> MD_CODE_SHIFT];
+                const float dx = (p4.x - pj[t].x) - o.x;
+                const float dy = (p4.y - pj[t].y) - o.y;
+                const float dz = (p4.z - pj[t].z) - o.z;
                 const float r2 = dx * dx + (dy * dy + dz * dz);
-                bool in = r2 < rclj2, in_rc = same_cut ? in : r2 < rc2;
-                if ((r2 > bl_lo && r2 < bl_hi) || (r2 > be_lo && r2 < be_hi)) {
-                    const double r2d = fp64_r2(S, i, j, code);
-                    in = r2d < cP.rclj2;
-                    in_rc = r2d < cP.rc2;
-                }
                 const bool macro = j > i;
-                nmol += (in_rc && macro) ? 1 : 0;
+                bool in = r2 < rclj2;
+                if (same_cut) {
+                    if (fabsf(r2 - rclj2) < band_lj) in = fp64_r2(S, i, j, ee[t] >> MD_CODE_SHIFT) < cP.rclj2;
+                } else {
+                    bool in_rc = r2 < rc2;
+                    if (fabsf(r2 - rclj2) < band_lj || fabsf(r2 - rc2) < band_rc) {
+                        const double r2d = fp64_r2(S, i, j, ee[t] >> MD_CODE_SHIFT);
+                        in = r2d < cP.rclj2;
+                        in_rc = r2d < cP.rc2;
+                    }
+                    nmol += (in_rc && macro) ? 1 : 0;
+                }
                 if (!in) continue;
                 if (!one_comp) {
                     const int gj = cP.comp[__float_as_int(pj[t].w)].ljoff;
@@ -561,7 +655,7 @@ __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __
                 const float lj12m6 = lj6 * lj6 - lj6;
                 const float scale = e24 * r2inv * (lj6 * lj6 + lj12m6);
                 const float f0 = dx * scale, f1 = dy * scale, f2 = dz * scale;
-                fx.add(f0); fy.add(f1); fz.add(f2);
+                gx += f0; gy += f1; gz += f2;
                 const float V0 = dx * f0, V1 = dy * f1, V2 = dz * f2;
                 vx += V0; vy += V1; vz += V2;
                 if (macro) {
@@ -570,7 +664,9 @@ __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __
                     ++npairs;
                 }
             }
+            fx.add(gx); fy.add(gy); fz.add(gz);
         }
+        if (same_cut) nmol = npairs;
         S.Fx[i] = fx.value(); S.Fy[i] = fy.value(); S.Fz[i] = fz.value();
         S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
         S.Vx[i] = 0.5 * (double)vx; S.Vy[i] = 0.5 * (double)vy; S.Vz[i] = 0.5 * (double)vz;
@@ -765,7 +861,7 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
 // ------------------------------------------------------------------ integration
 // FullMolecule::upd_preF; afterwards the FP32 local coordinates and the
 // displacement since the last list build (for the rebuild test).
-__global__ void k_pre(State S, double dt, float4* xlf, const double* rref, unsigned* disp_max) {
+__global__ void k_pre(State S, double dt, float4* xlf, const double* origin, const float4* xlref, unsigned* disp_max) {
     __shared__ float smax[8];
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float d2 = 0.f;
@@ -807,8 +903,14 @@ __global__ void k_pre(State S, double dt, float4* xlf, const double* rref, unsig
             S.qw[i] = q[0]; S.qx[i] = q[1]; S.qy[i] = q[2]; S.qz[i] = q[3];
             S.Lx[i] = L[0]; S.Ly[i] = L[1]; S.Lz[i] = L[2];
         }
-        make_local<float4>(S, i, xlf);
-        float ddx = (float)(rx - rref[3 * i]), ddy = (float)(ry - rref[3 * i + 1]), ddz = (float)(rz - rref[3 * i + 2]);
+        float4 p;
+        p.x = (float)(rx - origin[3 * i]);
+        p.y = (float)(ry - origin[3 * i + 1]);
+        p.z = (float)(rz - origin[3 * i + 2]);
+        const float4 q0 = xlref[i];
+        p.w = q0.w;
+        xlf[i] = p;
+        const float ddx = p.x - q0.x, ddy = p.y - q0.y, ddz = p.z - q0.z;
         d2 = ddx * ddx + ddy * ddy + ddz * ddz;
     }
     for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, o));
@@ -843,7 +945,7 @@ __global__ void k_sum_int(const int* a, int64_t n, unsigned long long* out) {
 // FullMolecule::upd_postF with the Leapfrog sums.
 __global__ void k_post(State S, double dt, double* partials, int pstride) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    double mv2 = 0.0, iw2 = 0.0, rot = 0.0, one = 0.0;
+    double mv2 = 0.0, iw2 = 0.0;
     if (i < S.n) {
         const CompDev& C = cP.comp[S.comp[i]];
         double dt_halve = 0.5 * dt;
@@ -869,13 +971,9 @@ __global__ void k_post(State S, double dt, double* partials, int pstride) {
                 iw2 += C.I[d] * w[d] * w[d];
             }
         }
-        rot = C.rot_dof;
-        one = 1.0;
     }
     warp_partial(partials, pstride, 12, mv2);
-    warp_partial(partials, pstride, 13, iw2);
-    warp_partial(partials, pstride, 14, one);
-    warp_partial(partials, pstride, 15, rot);
+    if (cP.any_rotation) warp_partial(partials, pstride, 13, iw2);
 }
 
 #include "md_adjoint.inc"
