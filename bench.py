@@ -13,7 +13,11 @@ forces, post-force half step and the Upot/virial/kinetic sums.
   e2e     the same metric through the C ABI from host buffers: upload of the
           phase space, the K steps with the per-step sums read back, and the
           download of the final phase space, all inside the timed region;
-  roofline  the pair kernel (dominant kernel) against the FP32 FMA rate;
+  roofline  the pair kernel (dominant kernel): algorithmic bytes per launch /
+          event-timed launch duration against the measured HBM copy
+          bandwidth, with the DRAM traffic scaled from an ncu capture;
+  roofline_fp32  the same launch as the reference's FlopCounter flops per
+          unique in-cutoff pair against the nominal FP32 FMA rate;
   cpu_baseline  the CPU oracle (C restatement of the reference's path, OpenMP
           C08 traversal) on all host cores on a bounded sample of the workload.
 
@@ -56,8 +60,12 @@ WORKLOADS = {
     "mix1m": (lambda: psm.mixture(1_000_000, 18.0, 300.0, seed=2026), 1.0, 9.118e-5,
               "2CLJQ/1CLJD 50/50 mixture, N=1,000,188, n=18 nm^-3, T=300 K, rc=1 nm, RF eps=1e10, dt=1 fs"),
 }
-DEFAULT_SKIN = {"lj4m": 0.3, "lj1m": 0.3, "lj32k": 0.3, "slab": 0.3, "mix1m": 0.1}
+DEFAULT_SKIN = {"lj4m": 0.25, "lj1m": 0.25, "lj32k": 0.3, "slab": 0.25, "mix1m": 0.1}
 FLOP_PER_PAIR_LJ = 39.0  # reference FlopCounter model: 31 per LJ site pair + 8 per molecule distance
+# DRAM bytes (read + write) of one k_force_lj32 launch per pair-candidate list entry, from an ncu
+# capture of the 1,000,188-molecule case (467.0 MB for 87.17 entries per molecule); traffic grows
+# with the entries read, so it is scaled by the live entry count.
+FORCE_DRAM_BYTES_PER_ENTRY = 467.0e6 / (1_000_188 * 87.17)
 
 
 # ---------------------------------------------------------------- CUDA events on the engine stream
@@ -275,6 +283,7 @@ def main():
     achieved = flops / (kt.force_ms * 1e-3) / 1e12
     list_bytes = kt.mean_candidates * n * 4.0
     hbm_bytes = list_bytes + n * (16 + 4 + 9 * 8)
+    traffic = FORCE_DRAM_BYTES_PER_ENTRY * kt.mean_candidates * n if a.precision == "mixed" else None
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     hbm_peak, hbm_src = 6800.0, "fallback"
     if os.path.exists(peaks_path):
@@ -312,15 +321,17 @@ def main():
             "config": {"workload": desc, "precision": a.precision, "skin": skin, "molecules": n,
                        "parallelism": f"replicas x{world}", "l2": "working set > L2 (GBs), no flush needed"},
             "gpu_launches": int(kt.launches_per_step * a.steps),
-            "roofline": {"bound": "fp32", "kernel": "k_force_lj<float>", "achieved": achieved, "peak": fp32_peak,
-                         "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
-                         "algorithmic": f"{FLOP_PER_PAIR_LJ:.0f} flop x {pairs} unique in-cutoff pairs per launch",
-                         "launch_ms": kt.force_ms,
-                         "peak_source": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 flop x 2070 MHz"},
-            "roofline_hbm": {"bound": "hbm", "achieved": hbm_bytes / (kt.force_ms * 1e-3) / 1e9, "peak": hbm_peak,
-                             "unit": "GB/s", "frac": hbm_bytes / (kt.force_ms * 1e-3) / 1e9 / hbm_peak,
-                             "peak_source": hbm_src,
-                             "algorithmic": "pair-candidate list (4 B/entry) + positions + outputs per launch"},
+            "roofline": {"bound": "hbm", "kernel": "k_force_lj32" if a.precision == "mixed" else "k_force_lj64",
+                         "achieved": hbm_bytes / (kt.force_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": hbm_bytes / (kt.force_ms * 1e-3) / 1e9 / hbm_peak,
+                         "traffic": traffic, "peak_source": hbm_src,
+                         "algorithmic": "per launch: 4 B per pair-candidate list entry + 16 B position + 4 B count"
+                                        " + 72 B F/M/Vi per molecule",
+                         "algorithmic_bytes": hbm_bytes, "launch_ms": kt.force_ms},
+            "roofline_fp32": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                              "frac": achieved / fp32_peak,
+                              "algorithmic": f"{FLOP_PER_PAIR_LJ:.0f} flop x {pairs} unique in-cutoff pairs per launch",
+                              "peak_source": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 flop x 2070 MHz"},
             "kernels_ms": {"force": kt.force_ms, "pre": kt.pre_ms, "post": kt.post_ms, "rebuild": kt.rebuild_ms},
             "pair_list": {"mean_candidates": kt.mean_candidates, "rebuilds": int(kt.rebuilds)},
             "physics": {"upot_per_molecule": fo.upot / n, "unique_lj_pairs": int(pairs)},
