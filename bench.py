@@ -60,6 +60,8 @@ WORKLOADS = {
     "mix1m": (lambda: psm.mixture(1_000_000, 18.0, 300.0, seed=2026), 1.0, 9.118e-5,
               "2CLJQ/1CLJD 50/50 mixture, N=1,000,188, n=18 nm^-3, T=300 K, rc=1 nm, RF eps=1e10, dt=1 fs"),
 }
+BATCH_DESC = ("512 independent periodic 1CLJ boxes, N log-uniform in [500, 20000] (seeded), rho* U[0.05, 0.85], "
+              "T* U[0.7, 1.3], rc=2.5, dt=0.002, graphs of 100 steps, skin and threads per molecule row autotuned")
 DEFAULT_SKIN = {"lj4m": 0.25, "lj1m": 0.25, "lj32k": 0.3, "slab": 0.25, "mix1m": 0.1}
 FLOP_PER_PAIR_LJ = 39.0  # reference FlopCounter model: 31 per LJ site pair + 8 per molecule distance
 # DRAM bytes (read + write) of one k_force_lj32 launch per pair-candidate list entry, from an ncu
@@ -191,7 +193,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="lj4m", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="lj4m", choices=sorted(WORKLOADS) + ["batch512"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--skin", type=float, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -239,11 +241,138 @@ def run_reference(a, rank):
     print(json.dumps(line))
 
 
+def batch_cpu_baseline(boxes, budget_s: float = 12.0) -> dict:
+    from oracle.oracle import Oracle
+    threads = os.cpu_count() or 1
+    done, t0, used = 0, time.perf_counter(), []
+    for b in boxes:
+        o = Oracle(b.to_phasespace(rc=2.5), 2.5, threads=threads)
+        o.rebin()
+        o.forces()
+        o.run(0.002, 20)
+        done += 20 * b.n
+        used.append(b.n)
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return {"value": done / el, "unit": "molecule-updates/s", "cores": threads, "kind": "port",
+            "sample": f"the first {len(used)} boxes of the batch ({sum(used)} molecules), 20 NVE steps each, one at a "
+                      f"time, {el:.1f} s with {threads} OpenMP threads"}
+
+
+def run_batch(a, rank, world, local, pg):
+    """Batch of independent boxes: md_batch throughput, per-box errors of the
+    mixed batch against the FP64 batch, and the same boxes run one at a time
+    through md_ctx in FP64 on the same GPU (a sample of them, timed)."""
+    from ls1gb300 import batch as B
+    from ls1gb300 import engine as E
+    cu = Cudart()
+    boxes = B.random_boxes(512, 500, 20000, seed=2024 + rank)
+    n = sum(b.n for b in boxes)
+    dt = 0.002
+    bt = B.Batch(boxes, 2.5, precision="mixed", device=local)
+    bt.forces()
+    tune = bt.autotune(dt, trial_steps=30)
+    bt.forces()
+    bt.run(dt, max(3, a.warmup), graph_steps=100, record=False)
+    stream = bt.stream()
+    clock = ClockSampler(local)
+    barrier(pg)
+    e0, e1 = cu.event(), cu.event()
+    clock.start()
+    cu.record(e0, stream)
+    rec = bt.run(dt, a.steps, graph_steps=100, record=True)
+    cu.record(e1, stream)
+    ms = cu.elapsed_ms(e0, e1)
+    clocks = clock.stop()
+    rebuilds = bt.rebuilds()
+    ms = max_over_ranks(pg, ms)
+    value = world * n * a.steps / (ms * 1e-3)
+    # per-box errors of the mixed batch at its final state: Upot and pressure
+    # p = (sum m v^2 + virial) / (3 V) from the last step's record against the
+    # FP64 forces of the same positions
+    fin = bt.molecules()
+    bt.close()
+    fboxes = [B.Box(L=b.L, r=np.ascontiguousarray(fin["r"][o:e]), v=np.ascontiguousarray(fin["v"][o:e]), rho=b.rho,
+                    T=b.T) for b, o, e in zip(boxes, bt.box_start[:-1], bt.box_start[1:])]
+    ref = B.Batch(fboxes, 2.5, precision="fp64", skin=0.3, device=local)
+    s64 = ref.forces()
+    ref.close()
+    vol = np.array([np.prod(b.L) for b in boxes])
+    nb = np.array([b.n for b in boxes], dtype=np.float64)
+    last = rec[-1]
+    du = np.abs(last[:, 0] - s64[:, 0]) / np.maximum(np.abs(s64[:, 0]), 1e-300)
+    p64 = (last[:, 2] + s64[:, 1]) / (3.0 * vol)
+    dp = np.abs(last[:, 1] - s64[:, 1]) / (3.0 * vol) / np.abs(p64)
+    # end to end through the C ABI: create + upload + first forces + K steps (per-step per-box sums) + download
+    t0 = time.perf_counter()
+    bt2 = B.Batch(boxes, 2.5, precision="mixed", skin=tune["skin"], threads_per_molecule=tune["threads_per_molecule"],
+                  device=local)
+    bt2.forces()
+    rec2 = bt2.run(dt, a.steps, graph_steps=100, record=True)
+    out = bt2.molecules()
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
+    bt2.close()
+    h2d = n * 6 * 8 + n * 8 + 8 * (len(boxes) + 1)
+    d2h = rec2.nbytes + sum(out[k].nbytes for k in out)
+    # one box at a time, FP64 md_ctx on the same GPU: a spread sample of 16 boxes, 100 steps each
+    order = np.argsort(nb)
+    sample = [int(order[k]) for k in np.linspace(0, len(boxes) - 1, 16).astype(int)]
+    upd, tot_ms = 0, 0.0
+    for k in sample:
+        eng = E.Engine(boxes[k].to_phasespace(rc=2.5), 2.5, precision="fp64", skin=0.3, device=local)
+        eng.forces()
+        eng.run(dt, 10, record=False)
+        st = eng.stream()
+        c0, c1 = cu.event(), cu.event()
+        cu.record(c0, st)
+        eng.run(dt, 100, record=True)
+        cu.record(c1, st)
+        tot_ms += cu.elapsed_ms(c0, c1)
+        upd += boxes[k].n * 100
+        eng.close()
+    seq = upd / (tot_ms * 1e-3)
+    cb = batch_cpu_baseline(boxes) if (rank == 0 and world == 1 and not a.no_cpu_baseline) else None
+    if rank == 0:
+        line = {
+            "metric": "molecule-updates/s", "value": value, "unit": "molecule-updates/s", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32-pairs/f64-state",
+            "data": "synthetic (seeded boxes on fcc sites, Maxwell-Boltzmann velocities)",
+            "config": {"workload": BATCH_DESC, "boxes": len(boxes), "molecules": n, "precision": "mixed",
+                       "autotune": tune, "parallelism": f"replicas x{world}",
+                       "l2": "working set > L2 (state + lists of 2.7M molecules), no flush needed"},
+            "gpu_launches": 16 * a.steps,  # per step: pre, check, 11 rebuild kernels (early exit unless due), force, post, box sums
+            "batch": {"rebuilds": rebuilds,
+                      "errors_vs_fp64": "per box at the final state: Upot from the last step's record and the "
+                                        "pressure (sum m v^2 + virial) / 3V against FP64 forces of the same positions",
+                      "upot_rel_err_max": float(du.max()), "upot_rel_err_median": float(np.median(du)),
+                      "pressure_rel_err_max": float(dp.max()), "pressure_rel_err_median": float(np.median(dp)),
+                      "one_at_a_time_fp64": {"value": seq, "unit": "molecule-updates/s",
+                                             "sample": "16 boxes spread over the N range, md_ctx FP64, 100 steps each"},
+                      "speedup_vs_one_at_a_time_fp64": value / seq},
+            "clocks": clocks,
+            "e2e": {"value": world * n * a.steps / e2e_s, "unit": "molecule-updates/s",
+                    "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps},
+            "cpu_baseline": cb,
+        }
+        print(json.dumps(line))
+
+
 def main():
     a = parse()
     rank, world, local, pg = dist_setup()
     if a.impl == "reference":
         run_reference(a, rank)
+        return
+    if a.workload == "batch512":
+        import build as engine_build
+        if rank == 0:
+            engine_build.build()
+        barrier(pg)
+        run_batch(a, rank, world, local, pg)
+        if pg is not None:
+            pg.destroy_process_group()
         return
     import build as engine_build
     if rank == 0:

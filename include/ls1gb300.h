@@ -215,6 +215,75 @@ typedef struct {
 int md_get_stream(md_ctx* ctx, void** stream);
 int md_time_kernels(md_ctx* ctx, int32_t reps, md_kernel_times* out);
 
+/* ---- batches of independent boxes (no counterpart in the reference, which
+ * runs one domain per process).  Many periodic boxes of single-centre LJ
+ * molecules (one component: eps, sigma, mass; rc_lj = rc) are advanced
+ * together: every kernel launch covers all boxes, a run is captured as CUDA
+ * graphs of `graph_steps` steps, and per-box Upot / virial / sum m v^2 are
+ * recorded every step.  Each box follows the md_ctx semantics of the same
+ * box run alone (LinkedCells + VectorizedCellProcessor::_loopBodyLJ,
+ * VectorizedCellProcessor.cpp:171-224; Leapfrog, Leapfrog.cpp:38-147).
+ *
+ * md_batch_create: box b spans [0, box_len[3b+d]) along d, periodic; every box
+ *   needs three list cells of edge (rc + skin) per axis (skin is lowered to fit;
+ *   a box shorter than 3 rc is an error).  skin < 0 picks 0.3 (or the largest
+ *   that fits); threads_per_molecule 0 picks 1.  On error *b is still set so
+ *   md_batch_last_error can be read; call md_batch_destroy in every case.
+ * md_batch_upload: molecules of box k are rows [box_start[k], box_start[k+1])
+ *   of r, v (n x 3, n = box_start[nbox]); ids may be NULL (1..n).
+ * md_batch_compute_forces: forces at the uploaded positions (the reference's
+ *   Simulation::prepare_start); out[nbox] (may be NULL) gets Upot, virial and
+ *   the number of interacting pairs of each box.
+ * md_batch_run: nsteps NVE Leapfrog steps; rec (may be NULL) is nsteps x nbox,
+ *   row-major by step.
+ * md_batch_download: upload order; any pointer may be NULL.
+ * md_batch_autotune: times `trial_steps` steps for each candidate pair of list
+ *   skin (list cell edge rc + skin: 0.1 ... 0.5 as the boxes allow) and threads
+ *   per molecule row (1, 2, 4; 1 only in FP64), restores the state after each
+ *   trial and keeps the fastest; out (may be NULL) lists every trial. */
+typedef struct md_batch md_batch;
+
+typedef struct {
+    int32_t nbox;
+    int32_t precision;            /* MD_PREC_FP64 or MD_PREC_MIXED */
+    const double* box_len;        /* nbox x 3 */
+    double rc;                    /* molecule-centre cut-off (also the LJ cut-off) */
+    double epsilon, sigma, mass;  /* the LJ centre */
+    int32_t shifted;              /* 1: LJ shifted to zero at rc (LJTS) */
+    int32_t threads_per_molecule; /* 0, 1, 2 or 4 */
+    double skin;                  /* pair-candidate list skin; < 0: default */
+    int32_t device;
+    int32_t reserved;
+} md_batch_config;
+
+typedef struct {
+    double upot;
+    double virial;
+    int64_t pairs;
+} md_box_sums;
+
+#define MD_BATCH_TUNE_MAX 16
+typedef struct {
+    double skin;                  /* chosen */
+    int32_t threads_per_molecule; /* chosen */
+    int32_t ntrials;
+    double ms_per_step;           /* of the chosen configuration */
+    double trial_skin[MD_BATCH_TUNE_MAX];
+    int32_t trial_tpm[MD_BATCH_TUNE_MAX];
+    double trial_ms_per_step[MD_BATCH_TUNE_MAX];
+} md_batch_tuning;
+
+int md_batch_create(md_batch** b, const md_batch_config* cfg);
+int md_batch_destroy(md_batch* b);
+const char* md_batch_last_error(const md_batch* b);
+int md_batch_upload(md_batch* b, const int64_t* box_start, const uint64_t* ids, const double* r, const double* v);
+int md_batch_compute_forces(md_batch* b, md_box_sums* out);
+int md_batch_run(md_batch* b, double dt, int32_t nsteps, int32_t graph_steps, md_step_record* rec);
+int md_batch_download(md_batch* b, uint64_t* ids, double* r, double* v, double* F);
+int md_batch_autotune(md_batch* b, double dt, int32_t trial_steps, md_batch_tuning* out);
+int md_batch_get_stream(md_batch* b, void** stream);
+int md_batch_rebuilds(md_batch* b, int64_t* count);
+
 #ifdef __cplusplus
 }
 #endif

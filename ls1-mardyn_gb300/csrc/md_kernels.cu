@@ -411,11 +411,16 @@ __global__ void k_permute(State dst, State src, const int* perm, const int* mcel
 // Local coordinates relative to the home-cell origin.  At a list rebuild the
 // origin (FP64) and the local coordinates then (FP32, for the displacement
 // test) are stored per molecule; every pre-force step recomputes the local
-// coordinates from the FP64 position.
+// coordinates from the FP64 position.  Slot n gets a position far outside
+// every box: candidate rows are padded with it.
 __global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, const unsigned* need) {
     if (need && !*need) return;
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= S.n) return;
+    if (i == S.n) {  // the far-away slot that pads candidate rows
+        xlf[i] = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(0));
+        return;
+    }
+    if (i > S.n) return;
     int h = S.home[i];
     int cx = h % cP.ln[0], cy = (h / cP.ln[0]) % cP.ln[1], cz = h / (cP.ln[0] * cP.ln[1]);
     double ox = cP.bmin[0] + cx * cP.lside[0], oy = cP.bmin[1] + cy * cP.lside[1], oz = cP.bmin[2] + cz * cP.lside[2];
@@ -442,21 +447,26 @@ __global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, con
 // rc before the next rebuild is missed.
 #define BL_WARPS 4
 #define BL_BUF 8
-__global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const float4* xl, const int* start,
-                                                              int ncells, uint32_t* nbr, int* nnb, int maxnb,
-                                                              float rl2, unsigned* status, int* need_max,
-                                                              const unsigned* need) {
-    if (!*need) return;
-    __shared__ float4 scand[BL_WARPS][32];
-    __shared__ uint32_t sent[BL_WARPS][32];
-    __shared__ uint32_t sbuf[BL_WARPS][32][BL_BUF + 1];  // +1: no bank conflicts between lanes
-    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c = blockIdx.x * BL_WARPS + wl;
-    if (c >= ncells) return;  // warp-uniform; only warp-level synchronisation below
-    const int hc[3] = {c % cP.ln[0], (c / cP.ln[0]) % cP.ln[1], c / (cP.ln[0] * cP.ln[1])};
-    const float side[3] = {(float)cP.lside[0], (float)cP.lside[1], (float)cP.lside[2]};
+// Geometry of one box's list grid: cells per axis, cell edges, periodicity,
+// and the global index of its first cell (boxes of a batch are numbered one
+// after another).
+struct ListGrid {
+    int ln[3];
+    float side[3];
+    bool per[3];
+    int base;
+};
+
+// Rows of the molecules of list cell `lc` (local index in grid g), built by
+// one warp; scand/sbuf are this warp's shared-memory staging areas.
+__device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, const int* start, const ListGrid& g,
+                                                int lc, uint32_t* nbr, int* nnb, int maxnb, float rl2,
+                                                unsigned* status, int* need_max, float4* scand,
+                                                uint32_t (*sbuf)[BL_BUF + 1], int lane) {
+    const int hc[3] = {lc % g.ln[0], (lc / g.ln[0]) % g.ln[1], lc / (g.ln[0] * g.ln[1])};
+    const int c = g.base + lc;
     const int b = start[c], e = start[c + 1];
-    uint32_t* buf = sbuf[wl][lane];
+    uint32_t* buf = sbuf[lane];
     for (int i0 = b; i0 < e; i0 += 32) {
         const int i = i0 + lane;
         const bool own = i < e;
@@ -472,43 +482,44 @@ __global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const f
                     bool skip = false;
                     for (int d = 0; d < 3; ++d) {
                         cc[d] = hc[d] + o[d];
-                        if (cc[d] < 0 || cc[d] >= cP.ln[d]) {
-                            if (!cP.periodic[d]) { skip = true; break; }
-                            cc[d] = (cc[d] + cP.ln[d]) % cP.ln[d];
+                        if (cc[d] < 0 || cc[d] >= g.ln[d]) {
+                            if (!g.per[d]) { skip = true; break; }
+                            cc[d] = (cc[d] + g.ln[d]) % g.ln[d];
                         }
                     }
                     if (skip) continue;
-                    const int cell = (cc[2] * cP.ln[1] + cc[1]) * cP.ln[0] + cc[0];
+                    const int cell = g.base + (cc[2] * g.ln[1] + cc[1]) * g.ln[0] + cc[0];
                     const uint32_t code = (uint32_t)((ox + 1) + 3 * (oy + 1) + 9 * (oz + 1));
-                    const float sx = ox * side[0], sy = oy * side[1], sz = oz * side[2];
+                    const float sx = ox * g.side[0], sy = oy * g.side[1], sz = oz * g.side[2];
                     const int nb0 = start[cell], ne = start[cell + 1];
                     for (int j0 = nb0; j0 < ne; j0 += 32) {
                         const int m = min(32, ne - j0);
                         __syncwarp();
                         if (lane < m) {
                             const float4 pj = xl[j0 + lane];
-                            scand[wl][lane] = make_float4(pj.x + sx, pj.y + sy, pj.z + sz, 0.f);
-                            sent[wl][lane] = (uint32_t)(j0 + lane) | (code << MD_CODE_SHIFT);
+                            scand[lane] = make_float4(pj.x + sx, pj.y + sy, pj.z + sz, 0.f);
                         }
                         __syncwarp();
-                        if (!own) continue;
+                        // append without branching: the entry is always stored at buf[nb] and
+                        // kept only on a hit; only the flush of a full buffer branches
+                        const uint32_t e0 = (uint32_t)j0 | (code << MD_CODE_SHIFT);
                         for (int t = 0; t < m; ++t) {
-                            const float4 q = scand[wl][t];
+                            const float4 q = scand[t];
                             const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
                             const float r2 = dx * dx + dy * dy + dz * dz;
-                            if (r2 < rl2 && j0 + t != i) {
-                                buf[nb++] = sent[wl][t];
-                                if (nb == BL_BUF) {
-                                    if (cnt + BL_BUF <= maxnb) {
-                                        uint4* dst = reinterpret_cast<uint4*>(row + cnt);
-                                        dst[0] = make_uint4(buf[0], buf[1], buf[2], buf[3]);
-                                        dst[1] = make_uint4(buf[4], buf[5], buf[6], buf[7]);
-                                    } else {
-                                        for (int u = 0; u < BL_BUF && cnt + u < maxnb; ++u) row[cnt + u] = buf[u];
-                                    }
-                                    cnt += BL_BUF;
-                                    nb = 0;
+                            const bool hit = own && r2 < rl2 && j0 + t != i;
+                            buf[nb] = e0 + (uint32_t)t;
+                            nb += hit ? 1 : 0;
+                            if (nb == BL_BUF) {
+                                if (cnt + BL_BUF <= maxnb) {
+                                    uint4* dst = reinterpret_cast<uint4*>(row + cnt);
+                                    dst[0] = make_uint4(buf[0], buf[1], buf[2], buf[3]);
+                                    dst[1] = make_uint4(buf[4], buf[5], buf[6], buf[7]);
+                                } else {
+                                    for (int u = 0; u < BL_BUF && cnt + u < maxnb; ++u) row[cnt + u] = buf[u];
                                 }
+                                cnt += BL_BUF;
+                                nb = 0;
                             }
                         }
                     }
@@ -516,6 +527,9 @@ __global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const f
         if (own) {
             for (int u = 0; u < nb && cnt + u < maxnb; ++u) row[cnt + u] = buf[u];
             cnt += nb;
+            // pad the row to a multiple of four with the far-away slot n (zero cell offset)
+            const uint32_t pad = (uint32_t)n | (13u << MD_CODE_SHIFT);
+            for (int u = cnt; u < ((cnt + 3) & ~3) && u < maxnb; ++u) row[u] = pad;
             nnb[i] = min(cnt, maxnb);
             if (cnt > maxnb) {
                 atomicOr(status, ST_LIST_OVERFLOW);
@@ -523,6 +537,37 @@ __global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const f
             }
         }
     }
+}
+
+// Owner-computes pair-candidate list over the 27 list cells around each
+// molecule's home cell (periodic wrap in periodic dimensions).  One warp per
+// home cell holds up to 32 of its molecules, one per lane.  For each
+// neighbour cell the warp stages 32 candidates at a time in shared memory
+// (coalesced load, already shifted into the home cell's frame); every lane
+// tests its molecule against the staged candidates (broadcast reads) and
+// appends hits to its own 8-entry shared-memory buffer, flushed as two
+// 16-byte stores into its row.  Rows are row-major (row i at i * maxnb,
+// maxnb a multiple of 4).  Candidate test in FP32 local coordinates against
+// (rc + skin)^2 enlarged by a relative 2e-4, so no pair that can come within
+// rc before the next rebuild is missed.
+__global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const float4* xl, const int* start,
+                                                              int ncells, uint32_t* nbr, int* nnb, int maxnb,
+                                                              float rl2, unsigned* status, int* need_max,
+                                                              const unsigned* need) {
+    if (!*need) return;
+    __shared__ float4 scand[BL_WARPS][32];
+    __shared__ uint32_t sbuf[BL_WARPS][32][BL_BUF + 1];  // +1: no bank conflicts between lanes
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * BL_WARPS + wl;
+    if (c >= ncells) return;  // warp-uniform; only warp-level synchronisation below
+    ListGrid g;
+    for (int d = 0; d < 3; ++d) {
+        g.ln[d] = cP.ln[d];
+        g.side[d] = (float)cP.lside[d];
+        g.per[d] = cP.periodic[d] != 0;
+    }
+    g.base = 0;
+    build_cell_rows(n, xl, start, g, c, nbr, nnb, maxnb, rl2, status, need_max, scand[wl], sbuf[wl], lane);
 }
 
 // ------------------------------------------------------------------ site cache
@@ -572,9 +617,6 @@ template <typename Real> struct R4;
 template <> struct R4<float> { typedef float4 t; };
 template <> struct R4<double> { typedef double4 t; };
 
-// Single-LJ-centre molecules (centre at the molecule origin): the hot path
-// of the 1CLJ benchmarks.  One thread per molecule, list entries streamed
-// column-major.
 // Single-LJ-centre molecules (centre at the molecule origin), FP32 pair
 // arithmetic: the hot kernel of the 1CLJ benchmarks.  One thread per
 // molecule streams its candidate row four entries per 16-byte load, gathers
@@ -677,6 +719,170 @@ __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __
     warp_partial(partials, pstride, 3, 0.0);
     warp_partial(partials, pstride, 4, (double)nmol);
     warp_partial(partials, pstride, 5, (double)npairs);
+    for (int sl = 6; sl < 12; ++sl) warp_partial(partials, pstride, sl, 0.0);
+}
+
+// FP64 re-decision of a pair near a cut-off, always evaluated in the frame of
+// the pair's smaller slot index, so that the two directions of a pair decide
+// alike (code 26 - c is the opposite cell offset of code c).
+__device__ __forceinline__ double fp64_r2_canon(const State& S, int i, int j, uint32_t code) {
+    return j > i ? fp64_r2(S, i, j, code) : fp64_r2(S, j, i, 26u - code);
+}
+
+// Candidate-row loads of the LJ kernels: the next 16-byte chunk of a row is
+// loaded one iteration ahead.  MD_LIST_LOAD_MODE 0: plain read-only load,
+// issued after the current chunk's position gathers; 1: issued first, with an
+// L2 prefetch-size hint of 256 bytes (rows are read sequentially); 2: as 1,
+// and the chunk bypasses L1 so that L1 keeps the neighbour positions.
+#ifndef MD_LIST_LOAD_MODE
+#define MD_LIST_LOAD_MODE 1
+#endif
+__device__ __forceinline__ uint4 ld_row_chunk(const uint4* p) {
+#if MD_LIST_LOAD_MODE == 0
+    return __ldg(p);
+#else
+    uint4 r;
+#if MD_LIST_LOAD_MODE == 2
+    asm("ld.global.nc.L1::no_allocate.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+#else
+    asm("ld.global.nc.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+#endif
+    return r;
+#endif
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// One candidate pair of the packed LJ loop below: lanes .x and .y of every
+// float2 are two different neighbours of the same molecule.  All arithmetic
+// between the distance and the accumulators runs on Blackwell's paired FP32
+// instructions (FFMA2/FADD2/FMUL2: two FP32 results per issue).  Pairs
+// outside the cut-off are masked (scale 0), not branched around.
+struct LjPack {
+    float2 gx, gy, gz;        // this group's force / eps24
+    float2 vx, vy, vz;        // sum d o f / eps24 over the molecule's pairs
+    float2 up, nin;           // sum (lj12 - lj6), in-cut-off pair count
+};
+
+__device__ __forceinline__ void lj_pack2(const State& S, int i, const float2 pix, const float2 piy, const float2 piz,
+                                         const float4 pa, const float4 pb, const float4 oa, const float4 ob,
+                                         uint32_t ea, uint32_t eb, const float2 ns2, const float rc2f,
+                                         const float band, LjPack& a) {
+    const float2 m1 = make_float2(-1.f, -1.f);
+    float2 dx = __ffma2_rn(make_float2(pa.x, pb.x), m1, pix);
+    float2 dy = __ffma2_rn(make_float2(pa.y, pb.y), m1, piy);
+    float2 dz = __ffma2_rn(make_float2(pa.z, pb.z), m1, piz);
+    dx = __fadd2_rn(dx, make_float2(oa.x, ob.x));
+    dy = __fadd2_rn(dy, make_float2(oa.y, ob.y));
+    dz = __fadd2_rn(dz, make_float2(oa.z, ob.z));
+    float2 r2 = __fmul2_rn(dz, dz);
+    r2 = __ffma2_rn(dy, dy, r2);
+    r2 = __ffma2_rn(dx, dx, r2);
+    bool ina = r2.x < rc2f, inb = r2.y < rc2f;
+    const bool nera = fabsf(r2.x - rc2f) < band, nerb = fabsf(r2.y - rc2f) < band;
+    if (nera || nerb) {
+        if (nera) ina = fp64_r2_canon(S, i, (int)(ea & MD_INDEX_MASK), ea >> MD_CODE_SHIFT) < cP.rclj2;
+        if (nerb) inb = fp64_r2_canon(S, i, (int)(eb & MD_INDEX_MASK), eb >> MD_CODE_SHIFT) < cP.rclj2;
+    }
+    const float2 msk = make_float2(ina ? 1.f : 0.f, inb ? 1.f : 0.f);
+    const float2 r2i = make_float2(rcp_approx(r2.x), rcp_approx(r2.y));
+    // VCP::_loopBodyLJ with eps24 factored out: u = lj12 - lj6, scale = (2 lj12 - lj6) / r^2
+    const float2 nlj2 = __fmul2_rn(ns2, r2i);            // -sigma^2 / r^2
+    const float2 nlj6 = __fmul2_rn(__fmul2_rn(nlj2, nlj2), nlj2);  // -lj6
+    const float2 u = __ffma2_rn(nlj6, nlj6, nlj6);
+    const float2 w = __ffma2_rn(nlj6, nlj6, u);
+    const float2 sc = __fmul2_rn(__fmul2_rn(r2i, msk), w);
+    const float2 f0 = __fmul2_rn(dx, sc), f1 = __fmul2_rn(dy, sc), f2 = __fmul2_rn(dz, sc);
+    a.gx = __fadd2_rn(a.gx, f0);
+    a.gy = __fadd2_rn(a.gy, f1);
+    a.gz = __fadd2_rn(a.gz, f2);
+    a.vx = __ffma2_rn(dx, f0, a.vx);
+    a.vy = __ffma2_rn(dy, f1, a.vy);
+    a.vz = __ffma2_rn(dz, f2, a.vz);
+    a.up = __ffma2_rn(u, msk, a.up);
+    a.nin = __fadd2_rn(a.nin, msk);
+}
+
+// Single-component, single-LJ-centre molecules with rc_lj = rc (the 1CLJ
+// benchmarks), FP32 pair arithmetic on paired FP32 instructions.  One thread
+// per molecule streams its candidate row 16 bytes (four entries) at a time;
+// rows are padded to a multiple of four with an entry that points at a far
+// away position (slot n), so the loop has no bounds tests.  Every pair is
+// evaluated from both sides with identical rounding (the FP32 distance is
+// antisymmetric and near-cut-off pairs are re-decided in one canonical
+// frame), so Upot, virial and the pair count are half the per-molecule
+// sums over all neighbours.  Force sums are Kahan-compensated per group of
+// four candidates; eps24 multiplies the sums once per molecule.
+__global__ void __launch_bounds__(256, 3) k_force_lj32x2(State S, const float4* __restrict__ xlf,
+                                                         const uint32_t* __restrict__ nbr,
+                                                         const int* __restrict__ nnb, int maxnb, double* partials,
+                                                         int pstride) {
+    __shared__ float4 nsoff[27];  // minus the offset of neighbour cell origin (code) from the home cell origin
+    if (threadIdx.x < 27) {
+        int t = threadIdx.x;
+        nsoff[t] = make_float4((float)(-(t % 3 - 1) * cP.lside[0]), (float)(-((t / 3) % 3 - 1) * cP.lside[1]),
+                               (float)(-(t / 9 - 1) * cP.lside[2]), 0.f);
+    }
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double up = 0.0, vir = 0.0, npairs = 0.0;
+    if (i < S.n) {
+        const float4 p4 = xlf[i];
+        const int gi = cP.comp[__float_as_int(p4.w)].ljoff;
+        const float e24 = (float)cP.eps24[gi * cP.nlj + gi], s2 = (float)cP.sig2[gi * cP.nlj + gi];
+        const double sh6 = cP.shift6[gi * cP.nlj + gi];
+        const float2 pix = make_float2(p4.x, p4.x), piy = make_float2(p4.y, p4.y), piz = make_float2(p4.z, p4.z);
+        const float2 ns2 = make_float2(-s2, -s2);
+        const float rc2f = cP.rclj2f, band = cP.band_hi_lj - cP.rclj2f;
+        const int cnt = nnb[i];
+        KSum fx, fy, fz;
+        fx.init(); fy.init(); fz.init();
+        LjPack a;
+        a.vx = a.vy = a.vz = a.up = a.nin = make_float2(0.f, 0.f);
+        const uint4* row = reinterpret_cast<const uint4*>(nbr + (size_t)i * maxnb);
+        uint4 nx = cnt > 0 ? ld_row_chunk(row) : make_uint4(0u, 0u, 0u, 0u);
+        for (int k = 0; k < cnt; k += 4) {
+            const uint4 e4 = nx;
+#if MD_LIST_LOAD_MODE != 0
+            if (k + 4 < cnt) nx = ld_row_chunk(row + (k >> 2) + 1);
+#endif
+            const float4 pa = __ldg(&xlf[e4.x & MD_INDEX_MASK]), pb = __ldg(&xlf[e4.y & MD_INDEX_MASK]);
+            const float4 pc = __ldg(&xlf[e4.z & MD_INDEX_MASK]), pd = __ldg(&xlf[e4.w & MD_INDEX_MASK]);
+#if MD_LIST_LOAD_MODE == 0
+            if (k + 4 < cnt) nx = ld_row_chunk(row + (k >> 2) + 1);
+#endif
+            a.gx = a.gy = a.gz = make_float2(0.f, 0.f);
+            lj_pack2(S, i, pix, piy, piz, pa, pb, nsoff[e4.x >> MD_CODE_SHIFT], nsoff[e4.y >> MD_CODE_SHIFT], e4.x, e4.y,
+                     ns2, rc2f, band, a);
+            lj_pack2(S, i, pix, piy, piz, pc, pd, nsoff[e4.z >> MD_CODE_SHIFT], nsoff[e4.w >> MD_CODE_SHIFT], e4.z, e4.w,
+                     ns2, rc2f, band, a);
+            fx.add(a.gx.x + a.gx.y);
+            fy.add(a.gy.x + a.gy.y);
+            fz.add(a.gz.x + a.gz.y);
+        }
+        const double e = (double)e24;
+        const double nin = (double)(a.nin.x + a.nin.y);
+        const double vx = e * (double)(a.vx.x + a.vx.y), vy = e * (double)(a.vy.x + a.vy.y),
+                     vz = e * (double)(a.vz.x + a.vz.y);
+        S.Fx[i] = e * fx.value(); S.Fy[i] = e * fy.value(); S.Fz[i] = e * fz.value();
+        S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
+        S.Vx[i] = 0.5 * vx; S.Vy[i] = 0.5 * vy; S.Vz[i] = 0.5 * vz;
+        up = 0.5 * (e * (double)(a.up.x + a.up.y) + sh6 * nin);
+        vir = 0.5 * (vx + vy + vz);
+        npairs = 0.5 * nin;
+    }
+    warp_partial(partials, pstride, 0, up);
+    warp_partial(partials, pstride, 1, 0.0);
+    warp_partial(partials, pstride, 2, vir);
+    warp_partial(partials, pstride, 3, 0.0);
+    warp_partial(partials, pstride, 4, npairs);
+    warp_partial(partials, pstride, 5, npairs);
     for (int sl = 6; sl < 12; ++sl) warp_partial(partials, pstride, sl, 0.0);
 }
 
@@ -952,17 +1158,15 @@ __global__ void k_post(State S, double dt, double* partials, int pstride) {
         double dtInv2m = dt_halve / C.m;
         double v[3] = {S.vx[i], S.vy[i], S.vz[i]};
         double F[3] = {S.Fx[i], S.Fy[i], S.Fz[i]};
-        double L[3] = {S.Lx[i], S.Ly[i], S.Lz[i]};
-        double M[3] = {S.Mx[i], S.My[i], S.Mz[i]};
         double v2 = 0.;
         for (int d = 0; d < 3; ++d) {
             v[d] += dtInv2m * F[d];
             v2 += v[d] * v[d];
-            L[d] += dt_halve * M[d];
         }
         mv2 = C.m * v2;
         S.vx[i] = v[0]; S.vy[i] = v[1]; S.vz[i] = v[2];
-        if (!C.skip_rot) {
+        if (!C.skip_rot) {  // L and M are only read for molecules that rotate
+            double L[3] = {S.Lx[i] + dt_halve * S.Mx[i], S.Ly[i] + dt_halve * S.My[i], S.Lz[i] + dt_halve * S.Mz[i]};
             S.Lx[i] = L[0]; S.Ly[i] = L[1]; S.Lz[i] = L[2];
             double w[3];
             qrotinv(S.qw[i], S.qx[i], S.qy[i], S.qz[i], L, w);
@@ -976,5 +1180,53 @@ __global__ void k_post(State S, double dt, double* partials, int pstride) {
     if (cP.any_rotation) warp_partial(partials, pstride, 13, iw2);
 }
 
+// upd_postF of step k fused with upd_preF of step k + 1 for systems where no
+// molecule rotates (both half kicks use the same F): the same FP64
+// operations in the same order as k_post followed by k_pre, one pass over
+// the state instead of two.
+__global__ void k_post_pre(State S, double dt, double* partials, int pstride, float4* xlf, const double* origin,
+                           const float4* xlref, unsigned* disp_max) {
+    __shared__ float smax[8];
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double mv2 = 0.0;
+    float d2 = 0.f;
+    if (i < S.n) {
+        const CompDev& C = cP.comp[S.comp[i]];
+        const double dt_halve = 0.5 * dt;
+        const double dtInv2m = dt_halve / C.m;
+        const double F[3] = {S.Fx[i], S.Fy[i], S.Fz[i]};
+        double v[3] = {S.vx[i], S.vy[i], S.vz[i]};
+        double v2 = 0.;
+        for (int d = 0; d < 3; ++d) {
+            v[d] += dtInv2m * F[d];
+            v2 += v[d] * v[d];
+        }
+        mv2 = C.m * v2;
+        for (int d = 0; d < 3; ++d) v[d] = v[d] + dtInv2m * F[d];
+        const double rx = S.rx[i] + dt * v[0], ry = S.ry[i] + dt * v[1], rz = S.rz[i] + dt * v[2];
+        S.vx[i] = v[0]; S.vy[i] = v[1]; S.vz[i] = v[2];
+        S.rx[i] = rx; S.ry[i] = ry; S.rz[i] = rz;
+        const float4 q0 = xlref[i];
+        float4 p;
+        p.x = (float)(rx - origin[3 * i]);
+        p.y = (float)(ry - origin[3 * i + 1]);
+        p.z = (float)(rz - origin[3 * i + 2]);
+        p.w = q0.w;
+        xlf[i] = p;
+        const float ddx = p.x - q0.x, ddy = p.y - q0.y, ddz = p.z - q0.z;
+        d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+    }
+    warp_partial(partials, pstride, 12, mv2);
+    for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, o));
+    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = d2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, smax[w]);
+        atomicMax(disp_max, __float_as_uint(m));
+    }
+}
+
 #include "md_adjoint.inc"
 #include "md_api.inc"
+#include "md_batch.inc"

@@ -70,6 +70,26 @@ class MdKernelTimes(C.Structure):
                 ("launches_per_step", C.c_int32), ("reserved", C.c_int32)]
 
 
+class MdBatchConfig(C.Structure):
+    _fields_ = [("nbox", C.c_int32), ("precision", C.c_int32), ("box_len", C.POINTER(C.c_double)),
+                ("rc", C.c_double), ("epsilon", C.c_double), ("sigma", C.c_double), ("mass", C.c_double),
+                ("shifted", C.c_int32), ("threads_per_molecule", C.c_int32), ("skin", C.c_double),
+                ("device", C.c_int32), ("reserved", C.c_int32)]
+
+
+class MdBoxSums(C.Structure):
+    _fields_ = [("upot", C.c_double), ("virial", C.c_double), ("pairs", C.c_int64)]
+
+
+MD_BATCH_TUNE_MAX = 16
+
+
+class MdBatchTuning(C.Structure):
+    _fields_ = [("skin", C.c_double), ("threads_per_molecule", C.c_int32), ("ntrials", C.c_int32),
+                ("ms_per_step", C.c_double), ("trial_skin", C.c_double * MD_BATCH_TUNE_MAX),
+                ("trial_tpm", C.c_int32 * MD_BATCH_TUNE_MAX), ("trial_ms_per_step", C.c_double * MD_BATCH_TUNE_MAX)]
+
+
 def dptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 

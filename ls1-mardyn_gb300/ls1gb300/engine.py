@@ -62,6 +62,17 @@ def load_library(path: str = LIB_PATH):
     L.md_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.md_adjoint.argtypes = [vp, d, d, vp, vp, vp, i32]
     L.md_time_kernels.argtypes = [vp, i32, C.POINTER(abi.MdKernelTimes)]
+    L.md_batch_create.argtypes = [C.POINTER(vp), C.POINTER(abi.MdBatchConfig)]
+    L.md_batch_destroy.argtypes = [vp]
+    L.md_batch_last_error.argtypes = [vp]
+    L.md_batch_last_error.restype = C.c_char_p
+    L.md_batch_upload.argtypes = [vp, vp, vp, dp, dp]
+    L.md_batch_compute_forces.argtypes = [vp, C.POINTER(abi.MdBoxSums)]
+    L.md_batch_run.argtypes = [vp, d, i32, i32, C.POINTER(abi.MdStepRecord)]
+    L.md_batch_download.argtypes = [vp, vp, dp, dp, dp]
+    L.md_batch_autotune.argtypes = [vp, d, i32, C.POINTER(abi.MdBatchTuning)]
+    L.md_batch_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.md_batch_rebuilds.argtypes = [vp, C.POINTER(i64)]
     _lib = L
     return L
 

@@ -62,6 +62,52 @@ int main(void) {
     assert sizes[8] == abi.MdForcesOut.site_pairs.offset
 
 
+def test_batch_struct_layouts_match_header():
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "ls1gb300.h"
+int main(void) {
+  printf("%zu %zu %zu\n", sizeof(md_batch_config), sizeof(md_box_sums), sizeof(md_batch_tuning));
+  printf("%zu %zu %zu %zu\n", offsetof(md_batch_config, box_len), offsetof(md_batch_config, skin),
+         offsetof(md_batch_config, device), offsetof(md_batch_tuning, trial_ms_per_step));
+  return 0;
+}
+'''
+    d = tempfile.mkdtemp()
+    with open(os.path.join(d, "t.c"), "w") as f:
+        f.write(src)
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), "-o", os.path.join(d, "t"), os.path.join(d, "t.c")],
+                   check=True)
+    out = [int(x) for x in subprocess.run([os.path.join(d, "t")], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert out[:3] == [ctypes.sizeof(t) for t in (abi.MdBatchConfig, abi.MdBoxSums, abi.MdBatchTuning)]
+    assert out[3:] == [abi.MdBatchConfig.box_len.offset, abi.MdBatchConfig.skin.offset,
+                       abi.MdBatchConfig.device.offset, abi.MdBatchTuning.trial_ms_per_step.offset]
+
+
+def test_batch_create_without_gpu_fails_cleanly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    import numpy as np
+    lib.md_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(abi.MdBatchConfig)]
+    lib.md_batch_destroy.argtypes = [ctypes.c_void_p]
+    lib.md_batch_last_error.argtypes = [ctypes.c_void_p]
+    lib.md_batch_last_error.restype = ctypes.c_char_p
+    L = np.full(6, 10.0)
+    cfg = abi.MdBatchConfig(nbox=2, precision=abi.MD_PREC_MIXED, box_len=L.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                            rc=2.5, epsilon=1.0, sigma=1.0, mass=1.0, skin=-1.0)
+    h = ctypes.c_void_p()
+    assert lib.md_batch_create(ctypes.byref(h), ctypes.byref(cfg)) == abi.MD_ERR_DEVICE
+    assert b"device" in lib.md_batch_last_error(h)
+    lib.md_batch_destroy(h)
+    cfg.rc = 4.0   # 10 < 3 rc: rejected before any device call
+    h = ctypes.c_void_p()
+    assert lib.md_batch_create(ctypes.byref(h), ctypes.byref(cfg)) == abi.MD_ERR_ARG
+    lib.md_batch_destroy(h)
+
+
 def test_create_without_gpu_fails_cleanly(lib):
     """Without a visible GPU md_create returns MD_ERR_CUDA instead of crashing."""
     import torch
