@@ -193,7 +193,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="lj4m", choices=sorted(WORKLOADS) + ["batch512"])
+    ap.add_argument("--workload", default="lj4m", choices=sorted(WORKLOADS) + ["batch512", "adjoint"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--skin", type=float, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -307,6 +307,7 @@ def run_batch(a, rank, world, local, pg):
     # end to end through the C ABI: create + upload + first forces + K steps (per-step per-box sums) + download
     t0 = time.perf_counter()
     bt2 = B.Batch(boxes, 2.5, precision="mixed", skin=tune["skin"], threads_per_molecule=tune["threads_per_molecule"],
+                  cell_occupancy=tune["cell_occupancy"],
                   device=local)
     bt2.forces()
     rec2 = bt2.run(dt, a.steps, graph_steps=100, record=True)
@@ -359,18 +360,108 @@ def run_batch(a, rank, world, local, pg):
         print(json.dumps(line))
 
 
+def _perturbed(ps, f: float):
+    """The phase space with every LJ eps, sigma and multipole magnitude scaled by f."""
+    import copy
+    q = ps.copy()
+    comps = copy.deepcopy(ps.components)
+    for c in comps:
+        for s in c.lj:
+            s.eps *= f
+            s.sigma *= f
+        for s in c.dipoles + c.quadrupoles:
+            s.abs *= f
+    q.components = comps
+    return q
+
+
+def run_adjoint(a, rank, world, local, pg):
+    """Forward and adjoint cost on the differentiation workload: 64 snapshots
+    each of 1CLJ (fcc 29^3 x 4 = 97,556 molecules, rho*=0.7, T*=1.1, rc=2.5) and
+    of the 2CLJQ/1CLJD mixture (97,556 molecules on the same lattice, rc=1 nm).  Per snapshot the loss is
+    L = (U - U*)^2 + w (P - P*)^2 with targets from the FP64 forward at +2 %
+    parameters; the forward is md_compute_forces (list build + pair kernel +
+    sums), the adjoint md_adjoint (pairs recomputed from the list; gradients
+    of L w.r.t. positions and eps, sigma, |Q|, |mu|), FP32 pair arithmetic with
+    FP64 accumulation."""
+    from ls1gb300 import engine as E
+    cu = Cudart()
+    mix = psm.mixture(100_000, 18.0, 300.0, seed=4)
+    systems = [("1CLJ fcc 29^3x4 = 97,556, rho*=0.7, T*=1.1, rc=2.5",
+                psm.lj_fcc(29, 0.7, 1.1, seed=4), 2.5, 0.002, 0.3),
+               (f"2CLJQ/1CLJD mixture on fcc 29^3x4 = {mix.n:,} sites (n=18 nm^-3, T=300 K, rc=1 nm)",
+                mix, 1.0, 9.118e-5, 0.1)]
+    out = []
+    for desc, ps, rc, dt, skin in systems:
+        n = ps.n
+        vol = float(np.prod(ps.box))
+        eng = E.Engine(ps, rc, precision="mixed", skin=skin, device=local)
+        eng.forces()
+        snaps = []
+        for _ in range(64):
+            eng.run(dt, 20, record=False)
+            snaps.append(eng.molecules())
+        eng.close()
+        w = 1.0
+        fwd, adj, losses = [], [], []
+        tgt_ps = _perturbed(ps, 1.02)
+        ev = E.Engine(ps, rc, precision="mixed", skin=skin, device=local)
+        et = E.Engine(tgt_ps, rc, precision="fp64", skin=skin, device=local)
+        st = ev.stream()
+        for m in snaps:
+            for e_, ps_ in ((ev, ps), (et, tgt_ps)):
+                q = ps_.copy()
+                order = np.argsort(m["ids"])
+                q.r, q.v, q.q, q.L = m["r"][order], m["v"][order], m["q"][order], m["L"][order]
+                q.ids, q.comp = m["ids"][order], m["comp"][order]
+                e_.upload(q)
+            ft = et.forces()
+            u_t, p_t = ft.upot, ft.virial / (3 * vol)
+            c0, c1, c2 = cu.event(), cu.event(), cu.event()
+            cu.record(c0, st)
+            fo = ev.forces()
+            cu.record(c1, st)
+            gu = 2.0 * (fo.upot - u_t)
+            gw = 2.0 * w * (fo.virial / (3 * vol) - p_t) / (3 * vol)
+            ev.adjoint(gu, gw)
+            cu.record(c2, st)
+            fwd.append(cu.elapsed_ms(c0, c1))
+            adj.append(cu.elapsed_ms(c1, c2))
+            losses.append((fo.upot - u_t) ** 2 + w * (fo.virial / (3 * vol) - p_t) ** 2)
+        kt = ev.time_kernels(10)
+        ev.close()
+        et.close()
+        f_ms, a_ms = float(np.mean(fwd[4:])), float(np.mean(adj[4:]))
+        out.append({"system": desc, "molecules": n, "snapshots": len(snaps),
+                    "call_forward_ms": f_ms, "call_adjoint_ms": a_ms, "call_adjoint_over_forward": a_ms / f_ms,
+                    "kernel_forward_ms": kt.force_ms, "kernel_adjoint_ms": kt.adjoint_ms,
+                    "adjoint_over_forward": kt.adjoint_ms / kt.force_ms, "mean_loss": float(np.mean(losses))})
+    if rank == 0:
+        print(json.dumps({"metric": "adjoint/forward cost", "value": max(o["adjoint_over_forward"] for o in out),
+                          "unit": "ratio", "higher_is_better": False, "n_gpus": world,
+                          "dtype": "f32-pairs/f64-accumulation", "data": "synthetic (seeded snapshots of NVE runs)",
+                          "config": {"workload": "64 snapshots each of 1CLJ N=97,556 and the 2CLJQ/1CLJD mixture "
+                                                 "N=97,556; loss (U-U*)^2 + w (P-P*)^2, targets from FP64 at +2 % "
+                                                 "parameters; CUDA events on the engine stream",
+                                     "value": "max over the two systems of adjoint pair-kernel time / forward "
+                                              "pair-kernel time on the same list; call_* are the whole ABI calls "
+                                              "per snapshot (md_compute_forces with its list build vs md_adjoint "
+                                              "with the n x 3 gradient copied to the host)"},
+                          "systems": out}))
+
+
 def main():
     a = parse()
     rank, world, local, pg = dist_setup()
     if a.impl == "reference":
         run_reference(a, rank)
         return
-    if a.workload == "batch512":
+    if a.workload in ("batch512", "adjoint"):
         import build as engine_build
         if rank == 0:
             engine_build.build()
         barrier(pg)
-        run_batch(a, rank, world, local, pg)
+        (run_batch if a.workload == "batch512" else run_adjoint)(a, rank, world, local, pg)
         if pg is not None:
             pg.destroy_process_group()
         return

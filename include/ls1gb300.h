@@ -210,6 +210,8 @@ typedef struct {
     int64_t rebuilds;         /* list rebuilds since md_create                          */
     int32_t launches_per_step;/* kernels one md_run step launches                       */
     int32_t reserved;
+    double adjoint_ms;        /* one md_adjoint kernel pass (gU = gW = 1, no gF),
+                                 without its host copies                                */
 } md_kernel_times;
 
 int md_get_stream(md_ctx* ctx, void** stream);
@@ -237,10 +239,11 @@ int md_time_kernels(md_ctx* ctx, int32_t reps, md_kernel_times* out);
  * md_batch_run: nsteps NVE Leapfrog steps; rec (may be NULL) is nsteps x nbox,
  *   row-major by step.
  * md_batch_download: upload order; any pointer may be NULL.
- * md_batch_autotune: times `trial_steps` steps for each candidate pair of list
- *   skin (list cell edge rc + skin: 0.1 ... 0.5 as the boxes allow) and threads
- *   per molecule row (1, 2, 4; 1 only in FP64), restores the state after each
- *   trial and keeps the fastest; out (may be NULL) lists every trial. */
+ * md_batch_autotune: coordinate descent over the list skin (list cell edge
+ *   rc + skin: 0.1 ... 0.5 as the boxes allow), the list-cell occupancy in
+ *   dilute boxes (0, 8, 16, 32) and the threads per molecule row (1, 2, 4; 1
+ *   only in FP64): `trial_steps` steps timed per candidate, the state restored
+ *   after each trial, the fastest kept; out (may be NULL) lists every trial. */
 typedef struct md_batch md_batch;
 
 typedef struct {
@@ -254,6 +257,7 @@ typedef struct {
     double skin;                  /* pair-candidate list skin; < 0: default */
     int32_t device;
     int32_t reserved;
+    double cell_occupancy;        /* > 0: dilute boxes get list cells of about this many molecules */
 } md_batch_config;
 
 typedef struct {
@@ -271,6 +275,8 @@ typedef struct {
     double trial_skin[MD_BATCH_TUNE_MAX];
     int32_t trial_tpm[MD_BATCH_TUNE_MAX];
     double trial_ms_per_step[MD_BATCH_TUNE_MAX];
+    double cell_occupancy;        /* chosen */
+    double trial_occupancy[MD_BATCH_TUNE_MAX];
 } md_batch_tuning;
 
 int md_batch_create(md_batch** b, const md_batch_config* cfg);

@@ -59,6 +59,24 @@ struct Params {
     float rc2f, rclj2f, band_lo, band_hi, band_lo_lj, band_hi_lj;
     CompDev comp[MD_MAXC];
     double eps24[MD_MAXLJ * MD_MAXLJ], sig2[MD_MAXLJ * MD_MAXLJ], shift6[MD_MAXLJ * MD_MAXLJ];
+    // FP32 copies for the mixed-precision pair kernels (no FP64 conversion per pair)
+    float eps24f[MD_MAXLJ * MD_MAXLJ], sig2f[MD_MAXLJ * MD_MAXLJ], shift6f[MD_MAXLJ * MD_MAXLJ];
+    float pf[MD_MAXC][MD_MAXS];
+};
+
+// parameter-table reads in the pair kernels' precision
+template <typename Real> struct PTab;
+template <> struct PTab<float> {
+    static __device__ __forceinline__ float eps24(const Params& P, int k) { return P.eps24f[k]; }
+    static __device__ __forceinline__ float sig2(const Params& P, int k) { return P.sig2f[k]; }
+    static __device__ __forceinline__ float shift6(const Params& P, int k) { return P.shift6f[k]; }
+    static __device__ __forceinline__ float p(const Params& P, int c, int s) { return P.pf[c][s]; }
+};
+template <> struct PTab<double> {
+    static __device__ __forceinline__ double eps24(const Params& P, int k) { return P.eps24[k]; }
+    static __device__ __forceinline__ double sig2(const Params& P, int k) { return P.sig2[k]; }
+    static __device__ __forceinline__ double shift6(const Params& P, int k) { return P.shift6[k]; }
+    static __device__ __forceinline__ double p(const Params& P, int c, int s) { return P.comp[c].p[s]; }
 };
 
 struct State {

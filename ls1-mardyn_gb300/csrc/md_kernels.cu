@@ -362,9 +362,15 @@ __global__ void k_list_scatter(int64_t n, const int* mcell, int* cursor, int* pe
 
 // Deterministic order inside each cell: one warp per cell ranks the cell's
 // slot indices (the atomic scatter leaves them in arbitrary order) and writes
-// them back sorted.  Cells of up to 64 molecules are ranked in registers;
-// larger cells fall back to a serial insertion sort by lane 0.
-__global__ void k_cell_sort(const int* start, int ncells, int* perm, const unsigned* need) {
+// them back sorted, by component first when `comp` is given (so the warps of
+// the pair kernels see runs of one component), then by previous slot.  Cells
+// of up to 64 molecules are ranked in registers; larger cells fall back to a
+// serial insertion sort by lane 0.
+__device__ __forceinline__ int cell_sort_key(const int* comp, int v) {
+    return comp ? (comp[v] << MD_CODE_SHIFT) | v : v;
+}
+
+__global__ void k_cell_sort(const int* start, int ncells, int* perm, const int* comp, const unsigned* need) {
     if (!*need) return;
     int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -372,8 +378,8 @@ __global__ void k_cell_sort(const int* start, int ncells, int* perm, const unsig
     int b = start[c], e = start[c + 1], m = e - b;
     if (m <= 1) return;
     if (m <= 64) {
-        int v0 = lane < m ? perm[b + lane] : 0x7fffffff;
-        int v1 = lane + 32 < m ? perm[b + lane + 32] : 0x7fffffff;
+        int v0 = lane < m ? cell_sort_key(comp, perm[b + lane]) : 0x7fffffff;
+        int v1 = lane + 32 < m ? cell_sort_key(comp, perm[b + lane + 32]) : 0x7fffffff;
         int r0 = 0, r1 = 0;
         for (int t = 0; t < 32; ++t) {
             int a0 = __shfl_sync(0xffffffffu, v0, t), a1 = __shfl_sync(0xffffffffu, v1, t);
@@ -381,15 +387,15 @@ __global__ void k_cell_sort(const int* start, int ncells, int* perm, const unsig
             r1 += (a0 < v1) + (a1 < v1);
         }
         __syncwarp();
-        if (lane < m) perm[b + r0] = v0;
-        if (lane + 32 < m) perm[b + r1] = v1;
+        if (lane < m) perm[b + r0] = v0 & (int)MD_INDEX_MASK;
+        if (lane + 32 < m) perm[b + r1] = v1 & (int)MD_INDEX_MASK;
         return;
     }
     if (lane == 0) {
         for (int k = b + 1; k < e; ++k) {
-            int v = perm[k];
+            const int v = perm[k], kv = cell_sort_key(comp, v);
             int q = k - 1;
-            while (q >= b && perm[q] > v) { perm[q + 1] = perm[q]; --q; }
+            while (q >= b && cell_sort_key(comp, perm[q]) > kv) { perm[q + 1] = perm[q]; --q; }
             perm[q + 1] = v;
         }
     }
@@ -434,17 +440,6 @@ __global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, con
     xlref[i] = p;
 }
 
-// Owner-computes pair-candidate list over the 27 list cells around each
-// molecule's home cell (periodic wrap in periodic dimensions).  One warp per
-// home cell holds up to 32 of its molecules, one per lane.  For each
-// neighbour cell the warp stages 32 candidates at a time in shared memory
-// (coalesced load, already shifted into the home cell's frame); every lane
-// tests its molecule against the staged candidates (broadcast reads) and
-// appends hits to its own 8-entry shared-memory buffer, flushed as two
-// 16-byte stores into its row.  Rows are row-major (row i at i * maxnb,
-// maxnb a multiple of 4).  Candidate test in FP32 local coordinates against
-// (rc + skin)^2 enlarged by a relative 2e-4, so no pair that can come within
-// rc before the next rebuild is missed.
 #define BL_WARPS 4
 #define BL_BUF 8
 // Geometry of one box's list grid: cells per axis, cell edges, periodicity,
@@ -458,20 +453,28 @@ struct ListGrid {
 };
 
 // Rows of the molecules of list cell `lc` (local index in grid g), built by
-// one warp; scand/sbuf are this warp's shared-memory staging areas.
+// one warp; sq (3 x 32 floats) and sbuf are this warp's shared-memory areas.
+// Each batch of up to 32 candidates of a neighbour cell is staged as negated,
+// shifted coordinates (unused slots far away); every lane tests its molecule
+// against them, two per paired FP32 instruction, into a hit mask, then
+// appends the hits in candidate order.
 __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, const int* start, const ListGrid& g,
                                                 int lc, uint32_t* nbr, int* nnb, int maxnb, float rl2,
-                                                unsigned* status, int* need_max, float4* scand,
+                                                unsigned* status, int* need_max, float* sq,
                                                 uint32_t (*sbuf)[BL_BUF + 1], int lane) {
     const int hc[3] = {lc % g.ln[0], (lc / g.ln[0]) % g.ln[1], lc / (g.ln[0] * g.ln[1])};
     const int c = g.base + lc;
     const int b = start[c], e = start[c + 1];
     uint32_t* buf = sbuf[lane];
+    float* sx = sq;
+    float* sy = sq + 32;
+    float* sz = sq + 64;
     for (int i0 = b; i0 < e; i0 += 32) {
         const int i = i0 + lane;
         const bool own = i < e;
         float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
         if (own) pi = xl[i];
+        const float2 pix = make_float2(pi.x, pi.x), piy = make_float2(pi.y, pi.y), piz = make_float2(pi.z, pi.z);
         int cnt = 0, nb = 0;
         uint32_t* row = nbr + (size_t)(own ? i : 0) * maxnb;
         for (int oz = -1; oz <= 1; ++oz)
@@ -490,26 +493,42 @@ __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, con
                     if (skip) continue;
                     const int cell = g.base + (cc[2] * g.ln[1] + cc[1]) * g.ln[0] + cc[0];
                     const uint32_t code = (uint32_t)((ox + 1) + 3 * (oy + 1) + 9 * (oz + 1));
-                    const float sx = ox * g.side[0], sy = oy * g.side[1], sz = oz * g.side[2];
+                    const float shx = ox * g.side[0], shy = oy * g.side[1], shz = oz * g.side[2];
                     const int nb0 = start[cell], ne = start[cell + 1];
                     for (int j0 = nb0; j0 < ne; j0 += 32) {
                         const int m = min(32, ne - j0);
                         __syncwarp();
                         if (lane < m) {
                             const float4 pj = xl[j0 + lane];
-                            scand[lane] = make_float4(pj.x + sx, pj.y + sy, pj.z + sz, 0.f);
+                            sx[lane] = -(pj.x + shx);
+                            sy[lane] = -(pj.y + shy);
+                            sz[lane] = -(pj.z + shz);
+                        } else {
+                            sx[lane] = 1e18f;
+                            sy[lane] = 1e18f;
+                            sz[lane] = 1e18f;
                         }
                         __syncwarp();
-                        // append without branching: the entry is always stored at buf[nb] and
-                        // kept only on a hit; only the flush of a full buffer branches
+                        uint32_t hits = 0u;
+                        const int mm = (m + 1) & ~1;  // pairs of staged slots; slot m (if odd) is far away
+#pragma unroll 4
+                        for (int t = 0; t < mm; t += 2) {
+                            const float2 dx = __fadd2_rn(pix, *reinterpret_cast<const float2*>(sx + t));
+                            const float2 dy = __fadd2_rn(piy, *reinterpret_cast<const float2*>(sy + t));
+                            const float2 dz = __fadd2_rn(piz, *reinterpret_cast<const float2*>(sz + t));
+                            float2 r2 = __fmul2_rn(dz, dz);
+                            r2 = __ffma2_rn(dy, dy, r2);
+                            r2 = __ffma2_rn(dx, dx, r2);
+                            hits |= (r2.x < rl2 ? 1u : 0u) << t;
+                            hits |= (r2.y < rl2 ? 1u : 0u) << (t + 1);
+                        }
+                        if (!own) hits = 0u;
+                        if (i >= j0 && i < j0 + m) hits &= ~(1u << (i - j0));  // not the molecule itself
                         const uint32_t e0 = (uint32_t)j0 | (code << MD_CODE_SHIFT);
-                        for (int t = 0; t < m; ++t) {
-                            const float4 q = scand[t];
-                            const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
-                            const float r2 = dx * dx + dy * dy + dz * dz;
-                            const bool hit = own && r2 < rl2 && j0 + t != i;
-                            buf[nb] = e0 + (uint32_t)t;
-                            nb += hit ? 1 : 0;
+                        while (hits) {
+                            const int t = __ffs(hits) - 1;
+                            hits &= hits - 1u;
+                            buf[nb++] = e0 + (uint32_t)t;
                             if (nb == BL_BUF) {
                                 if (cnt + BL_BUF <= maxnb) {
                                     uint4* dst = reinterpret_cast<uint4*>(row + cnt);
@@ -544,10 +563,10 @@ __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, con
 // home cell holds up to 32 of its molecules, one per lane.  For each
 // neighbour cell the warp stages 32 candidates at a time in shared memory
 // (coalesced load, already shifted into the home cell's frame); every lane
-// tests its molecule against the staged candidates (broadcast reads) and
-// appends hits to its own 8-entry shared-memory buffer, flushed as two
-// 16-byte stores into its row.  Rows are row-major (row i at i * maxnb,
-// maxnb a multiple of 4).  Candidate test in FP32 local coordinates against
+// tests its molecule against the staged candidates (broadcast reads, two
+// per paired FP32 instruction) and appends hits to its own 8-entry
+// shared-memory buffer, flushed as two 16-byte stores into its row.  Rows
+// are row-major (row i at i * maxnb, maxnb a multiple of 4).  Candidate test in FP32 local coordinates against
 // (rc + skin)^2 enlarged by a relative 2e-4, so no pair that can come within
 // rc before the next rebuild is missed.
 __global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const float4* xl, const int* start,
@@ -555,7 +574,7 @@ __global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const f
                                                               float rl2, unsigned* status, int* need_max,
                                                               const unsigned* need) {
     if (!*need) return;
-    __shared__ float4 scand[BL_WARPS][32];
+    __shared__ __align__(16) float sq[BL_WARPS][3][32];
     __shared__ uint32_t sbuf[BL_WARPS][32][BL_BUF + 1];  // +1: no bank conflicts between lanes
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = blockIdx.x * BL_WARPS + wl;
@@ -567,7 +586,7 @@ __global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const f
         g.per[d] = cP.periodic[d] != 0;
     }
     g.base = 0;
-    build_cell_rows(n, xl, start, g, c, nbr, nnb, maxnb, rl2, status, need_max, scand[wl], sbuf[wl], lane);
+    build_cell_rows(n, xl, start, g, c, nbr, nnb, maxnb, rl2, status, need_max, &sq[wl][0][0], sbuf[wl], lane);
 }
 
 // ------------------------------------------------------------------ site cache
@@ -730,26 +749,54 @@ __device__ __forceinline__ double fp64_r2_canon(const State& S, int i, int j, ui
 }
 
 // Candidate-row loads of the LJ kernels: the next 16-byte chunk of a row is
-// loaded one iteration ahead.  MD_LIST_LOAD_MODE 0: plain read-only load,
-// issued after the current chunk's position gathers; 1: issued first, with an
-// L2 prefetch-size hint of 256 bytes (rows are read sequentially); 2: as 1,
-// and the chunk bypasses L1 so that L1 keeps the neighbour positions.
+// loaded one iteration ahead with an L2 prefetch-size hint of 256 bytes (rows
+// are read sequentially).  MD_LIST_LOAD_MODE 3 also marks the row data
+// evict-first in L2 (it is read once per launch), so that L2 keeps the
+// neighbour positions; MD_POS_HINT 1 marks the position gathers evict-last.
 #ifndef MD_LIST_LOAD_MODE
 #define MD_LIST_LOAD_MODE 1
 #endif
-__device__ __forceinline__ uint4 ld_row_chunk(const uint4* p) {
-#if MD_LIST_LOAD_MODE == 0
-    return __ldg(p);
-#else
+#ifndef MD_POS_HINT
+#define MD_POS_HINT 0
+#endif
+__device__ __forceinline__ uint64_t l2_policy_first() {
+    uint64_t p = 0;
+#if MD_LIST_LOAD_MODE == 3
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+#endif
+    return p;
+}
+
+__device__ __forceinline__ uint64_t l2_policy_last() {
+    uint64_t p = 0;
+#if MD_POS_HINT == 1
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+#endif
+    return p;
+}
+
+__device__ __forceinline__ uint4 ld_row_chunk(const uint4* p, uint64_t pol) {
     uint4 r;
-#if MD_LIST_LOAD_MODE == 2
-    asm("ld.global.nc.L1::no_allocate.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4];"
-        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+#if MD_LIST_LOAD_MODE == 3
+    asm("ld.global.nc.L2::cache_hint.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p), "l"(pol));
 #else
+    (void)pol;
     asm("ld.global.nc.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4];"
         : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
 #endif
     return r;
+}
+
+__device__ __forceinline__ float4 ld_pos(const float4* p, uint64_t pol) {
+#if MD_POS_HINT == 1
+    float4 r;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p), "l"(pol));
+    return r;
+#else
+    (void)pol;
+    return __ldg(p);
 #endif
 }
 
@@ -770,10 +817,56 @@ struct LjPack {
     float2 up, nin;           // sum (lj12 - lj6), in-cut-off pair count
 };
 
-__device__ __forceinline__ void lj_pack2(const State& S, int i, const float2 pix, const float2 piy, const float2 piz,
+// Candidates whose FP32 r^2 lies within the FP64 re-decision band of the
+// cut-off are left out of the packed loop and handled after it (keeping the
+// FP64 code out of the loop's register budget): up to MD_AMB of them are
+// remembered; with more, the row is scanned again for them.
+#define MD_AMB 4
+struct AmbList {
+    uint32_t e[MD_AMB];
+    int n;
+};
+
+__device__ __forceinline__ void amb_push(AmbList& am, uint32_t e) {
+    if (am.n < MD_AMB) am.e[am.n] = e;
+    ++am.n;
+}
+
+// The LJ pair of a deferred candidate found inside the cut-off, in the
+// packed loop's formulas (eps24 factored out), added to lane .x.
+__device__ __forceinline__ void lj_one(float dx, float dy, float dz, float r2, float s2, KSum& fx, KSum& fy, KSum& fz,
+                                       LjPack& a) {
+    const float r2i = rcp_approx(r2);
+    const float nlj2 = -s2 * r2i;
+    const float nlj6 = (nlj2 * nlj2) * nlj2;
+    const float u = fmaf(nlj6, nlj6, nlj6);
+    const float w = fmaf(nlj6, nlj6, u);
+    const float sc = r2i * w;
+    const float f0 = dx * sc, f1 = dy * sc, f2 = dz * sc;
+    fx.add(f0); fy.add(f1); fz.add(f2);
+    a.vx.x = fmaf(dx, f0, a.vx.x);
+    a.vy.x = fmaf(dy, f1, a.vy.x);
+    a.vz.x = fmaf(dz, f2, a.vz.x);
+    a.up.x += u;
+    a.nin.x += 1.f;
+}
+
+// FP32 squared distance with the packed loop's operation order:
+// d = (p_i - p_j) + o per axis, r^2 = dx dx + (dy dy + dz dz) fused.
+__device__ __forceinline__ float r2_scalar(const float4 pi, const float4 pj, float ox, float oy, float oz, float& dx,
+                                           float& dy, float& dz) {
+    dx = __fadd_rn(fmaf(pj.x, -1.f, pi.x), ox);
+    dy = __fadd_rn(fmaf(pj.y, -1.f, pi.y), oy);
+    dz = __fadd_rn(fmaf(pj.z, -1.f, pi.z), oz);
+    float r2 = __fmul_rn(dz, dz);
+    r2 = fmaf(dy, dy, r2);
+    return fmaf(dx, dx, r2);
+}
+
+__device__ __forceinline__ void lj_pack2(const float2 pix, const float2 piy, const float2 piz,
                                          const float4 pa, const float4 pb, const float4 oa, const float4 ob,
                                          uint32_t ea, uint32_t eb, const float2 ns2, const float rc2f,
-                                         const float band, LjPack& a) {
+                                         const float band, LjPack& a, AmbList& am) {
     const float2 m1 = make_float2(-1.f, -1.f);
     float2 dx = __ffma2_rn(make_float2(pa.x, pb.x), m1, pix);
     float2 dy = __ffma2_rn(make_float2(pa.y, pb.y), m1, piy);
@@ -786,9 +879,9 @@ __device__ __forceinline__ void lj_pack2(const State& S, int i, const float2 pix
     r2 = __ffma2_rn(dx, dx, r2);
     bool ina = r2.x < rc2f, inb = r2.y < rc2f;
     const bool nera = fabsf(r2.x - rc2f) < band, nerb = fabsf(r2.y - rc2f) < band;
-    if (nera || nerb) {
-        if (nera) ina = fp64_r2_canon(S, i, (int)(ea & MD_INDEX_MASK), ea >> MD_CODE_SHIFT) < cP.rclj2;
-        if (nerb) inb = fp64_r2_canon(S, i, (int)(eb & MD_INDEX_MASK), eb >> MD_CODE_SHIFT) < cP.rclj2;
+    if (nera || nerb) {  // decided in FP64 after the loop
+        if (nera) { ina = false; amb_push(am, ea); }
+        if (nerb) { inb = false; amb_push(am, eb); }
     }
     const float2 msk = make_float2(ina ? 1.f : 0.f, inb ? 1.f : 0.f);
     const float2 r2i = make_float2(rcp_approx(r2.x), rcp_approx(r2.y));
@@ -819,7 +912,13 @@ __device__ __forceinline__ void lj_pack2(const State& S, int i, const float2 pix
 // frame), so Upot, virial and the pair count are half the per-molecule
 // sums over all neighbours.  Force sums are Kahan-compensated per group of
 // four candidates; eps24 multiplies the sums once per molecule.
-__global__ void __launch_bounds__(256, 3) k_force_lj32x2(State S, const float4* __restrict__ xlf,
+#ifndef MD_LJ_GROUP
+#define MD_LJ_GROUP 4  // candidates per iteration of k_force_lj32x2 (4 or 8)
+#endif
+#ifndef MD_LJX2_MIN_BLOCKS
+#define MD_LJX2_MIN_BLOCKS 3  // blocks of 256 per SM the register budget is sized for
+#endif
+__global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State S, const float4* __restrict__ xlf,
                                                          const uint32_t* __restrict__ nbr,
                                                          const int* __restrict__ nnb, int maxnb, double* partials,
                                                          int pstride) {
@@ -845,26 +944,72 @@ __global__ void __launch_bounds__(256, 3) k_force_lj32x2(State S, const float4* 
         fx.init(); fy.init(); fz.init();
         LjPack a;
         a.vx = a.vy = a.vz = a.up = a.nin = make_float2(0.f, 0.f);
+        AmbList am;
+        am.n = 0;
         const uint4* row = reinterpret_cast<const uint4*>(nbr + (size_t)i * maxnb);
-        uint4 nx = cnt > 0 ? ld_row_chunk(row) : make_uint4(0u, 0u, 0u, 0u);
-        for (int k = 0; k < cnt; k += 4) {
-            const uint4 e4 = nx;
-#if MD_LIST_LOAD_MODE != 0
-            if (k + 4 < cnt) nx = ld_row_chunk(row + (k >> 2) + 1);
-#endif
-            const float4 pa = __ldg(&xlf[e4.x & MD_INDEX_MASK]), pb = __ldg(&xlf[e4.y & MD_INDEX_MASK]);
-            const float4 pc = __ldg(&xlf[e4.z & MD_INDEX_MASK]), pd = __ldg(&xlf[e4.w & MD_INDEX_MASK]);
-#if MD_LIST_LOAD_MODE == 0
-            if (k + 4 < cnt) nx = ld_row_chunk(row + (k >> 2) + 1);
-#endif
+        const uint64_t pol_row = l2_policy_first(), pol_pos = l2_policy_last();
+#if MD_LJ_GROUP == 8
+        // two chunks (eight candidates) per iteration; rows are padded to a multiple of eight
+        uint4 nx = cnt > 0 ? ld_row_chunk(row, pol_row) : make_uint4(0u, 0u, 0u, 0u);
+        uint4 ny = cnt > 4 ? ld_row_chunk(row + 1, pol_row) : make_uint4(0u, 0u, 0u, 0u);
+        for (int k = 0; k < cnt; k += 8) {
+            const uint4 e4 = nx, f4 = ny;
+            if (k + 8 < cnt) nx = ld_row_chunk(row + (k >> 2) + 2, pol_row);
+            if (k + 12 < cnt) ny = ld_row_chunk(row + (k >> 2) + 3, pol_row);
+            const bool two = k + 4 < cnt;
+            const float4 pa = ld_pos(&xlf[e4.x & MD_INDEX_MASK], pol_pos), pb = ld_pos(&xlf[e4.y & MD_INDEX_MASK], pol_pos);
+            const float4 pc = ld_pos(&xlf[e4.z & MD_INDEX_MASK], pol_pos), pd = ld_pos(&xlf[e4.w & MD_INDEX_MASK], pol_pos);
+            const uint4 g4 = f4;
+            float4 qa, qb, qc, qd;
+            if (two) {
+                qa = ld_pos(&xlf[g4.x & MD_INDEX_MASK], pol_pos); qb = ld_pos(&xlf[g4.y & MD_INDEX_MASK], pol_pos);
+                qc = ld_pos(&xlf[g4.z & MD_INDEX_MASK], pol_pos); qd = ld_pos(&xlf[g4.w & MD_INDEX_MASK], pol_pos);
+            }
             a.gx = a.gy = a.gz = make_float2(0.f, 0.f);
-            lj_pack2(S, i, pix, piy, piz, pa, pb, nsoff[e4.x >> MD_CODE_SHIFT], nsoff[e4.y >> MD_CODE_SHIFT], e4.x, e4.y,
-                     ns2, rc2f, band, a);
-            lj_pack2(S, i, pix, piy, piz, pc, pd, nsoff[e4.z >> MD_CODE_SHIFT], nsoff[e4.w >> MD_CODE_SHIFT], e4.z, e4.w,
-                     ns2, rc2f, band, a);
+            lj_pack2(pix, piy, piz, pa, pb, nsoff[e4.x >> MD_CODE_SHIFT], nsoff[e4.y >> MD_CODE_SHIFT], e4.x, e4.y,
+                     ns2, rc2f, band, a, am);
+            lj_pack2(pix, piy, piz, pc, pd, nsoff[e4.z >> MD_CODE_SHIFT], nsoff[e4.w >> MD_CODE_SHIFT], e4.z, e4.w,
+                     ns2, rc2f, band, a, am);
+            if (two) {
+                lj_pack2(pix, piy, piz, qa, qb, nsoff[g4.x >> MD_CODE_SHIFT], nsoff[g4.y >> MD_CODE_SHIFT], g4.x,
+                         g4.y, ns2, rc2f, band, a, am);
+                lj_pack2(pix, piy, piz, qc, qd, nsoff[g4.z >> MD_CODE_SHIFT], nsoff[g4.w >> MD_CODE_SHIFT], g4.z,
+                         g4.w, ns2, rc2f, band, a, am);
+            }
             fx.add(a.gx.x + a.gx.y);
             fy.add(a.gy.x + a.gy.y);
             fz.add(a.gz.x + a.gz.y);
+        }
+#else
+        uint4 nx = cnt > 0 ? ld_row_chunk(row, pol_row) : make_uint4(0u, 0u, 0u, 0u);
+        for (int k = 0; k < cnt; k += 4) {
+            const uint4 e4 = nx;
+            if (k + 4 < cnt) nx = ld_row_chunk(row + (k >> 2) + 1, pol_row);
+            const float4 pa = ld_pos(&xlf[e4.x & MD_INDEX_MASK], pol_pos), pb = ld_pos(&xlf[e4.y & MD_INDEX_MASK], pol_pos);
+            const float4 pc = ld_pos(&xlf[e4.z & MD_INDEX_MASK], pol_pos), pd = ld_pos(&xlf[e4.w & MD_INDEX_MASK], pol_pos);
+            a.gx = a.gy = a.gz = make_float2(0.f, 0.f);
+            lj_pack2(pix, piy, piz, pa, pb, nsoff[e4.x >> MD_CODE_SHIFT], nsoff[e4.y >> MD_CODE_SHIFT], e4.x, e4.y,
+                     ns2, rc2f, band, a, am);
+            lj_pack2(pix, piy, piz, pc, pd, nsoff[e4.z >> MD_CODE_SHIFT], nsoff[e4.w >> MD_CODE_SHIFT], e4.z, e4.w,
+                     ns2, rc2f, band, a, am);
+            fx.add(a.gx.x + a.gx.y);
+            fy.add(a.gy.x + a.gy.y);
+            fz.add(a.gz.x + a.gz.y);
+        }
+#endif
+        if (am.n > 0) {  // near-cut-off candidates: FP64 decision in the canonical frame
+            const bool listed = am.n <= MD_AMB;
+            const int m = listed ? am.n : cnt;
+            for (int t = 0; t < m; ++t) {
+                const uint32_t en = listed ? am.e[t] : nbr[(size_t)i * maxnb + t];
+                const int j = (int)(en & MD_INDEX_MASK);
+                const uint32_t code = en >> MD_CODE_SHIFT;
+                const float4 o = nsoff[code];
+                float dx, dy, dz;
+                const float r2 = r2_scalar(p4, __ldg(&xlf[j]), o.x, o.y, o.z, dx, dy, dz);
+                if (!(fabsf(r2 - rc2f) < band)) continue;  // (row scan) not near the cut-off
+                if (fp64_r2_canon(S, i, j, code) < cP.rclj2) lj_one(dx, dy, dz, r2, s2, fx, fy, fz, a);
+            }
         }
         const double e = (double)e24;
         const double nin = (double)(a.nin.x + a.nin.y);
@@ -1030,13 +1175,14 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
                     if (ka == SK_LJ) {
                         int ga = A.ljoff + a, gb = B.ljoff + b;
                         Real s2r = dsite[0] * dsite[0] + (dsite[1] * dsite[1] + dsite[2] * dsite[2]);
-                        lj_pair<Real>(dsite, md, s2r, (Real)cP.eps24[ga * cP.nlj + gb], (Real)cP.sig2[ga * cP.nlj + gb],
-                                      (Real)cP.shift6[ga * cP.nlj + gb], f, Vp, u);
+                        lj_pair<Real>(dsite, md, s2r, PTab<Real>::eps24(cP, ga * cP.nlj + gb),
+                                      PTab<Real>::sig2(cP, ga * cP.nlj + gb), PTab<Real>::shift6(cP, ga * cP.nlj + gb), f,
+                                      Vp, u);
                         if (macro) u6.add(u);
                         kind = 0;
                     } else {
-                        kind = multipole_pair<Real>(ka, kb, dsite, md, (Real)A.p[a], ea, (Real)B.p[b], eb, epsRF, f, Vp,
-                                                    T, u, urf);
+                        kind = multipole_pair<Real>(ka, kb, dsite, md, PTab<Real>::p(cP, ci, a), ea,
+                                                    PTab<Real>::p(cP, cj, b), eb, epsRF, f, Vp, T, u, urf);
                         if (macro) { ux.add(u); rf.add(urf); }
                     }
                     for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }

@@ -67,14 +67,14 @@ class MdStepRecord(C.Structure):
 class MdKernelTimes(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("pre_ms", C.c_double), ("post_ms", C.c_double),
                 ("rebuild_ms", C.c_double), ("mean_candidates", C.c_double), ("rebuilds", C.c_int64),
-                ("launches_per_step", C.c_int32), ("reserved", C.c_int32)]
+                ("launches_per_step", C.c_int32), ("reserved", C.c_int32), ("adjoint_ms", C.c_double)]
 
 
 class MdBatchConfig(C.Structure):
     _fields_ = [("nbox", C.c_int32), ("precision", C.c_int32), ("box_len", C.POINTER(C.c_double)),
                 ("rc", C.c_double), ("epsilon", C.c_double), ("sigma", C.c_double), ("mass", C.c_double),
                 ("shifted", C.c_int32), ("threads_per_molecule", C.c_int32), ("skin", C.c_double),
-                ("device", C.c_int32), ("reserved", C.c_int32)]
+                ("device", C.c_int32), ("reserved", C.c_int32), ("cell_occupancy", C.c_double)]
 
 
 class MdBoxSums(C.Structure):
@@ -87,7 +87,8 @@ MD_BATCH_TUNE_MAX = 16
 class MdBatchTuning(C.Structure):
     _fields_ = [("skin", C.c_double), ("threads_per_molecule", C.c_int32), ("ntrials", C.c_int32),
                 ("ms_per_step", C.c_double), ("trial_skin", C.c_double * MD_BATCH_TUNE_MAX),
-                ("trial_tpm", C.c_int32 * MD_BATCH_TUNE_MAX), ("trial_ms_per_step", C.c_double * MD_BATCH_TUNE_MAX)]
+                ("trial_tpm", C.c_int32 * MD_BATCH_TUNE_MAX), ("trial_ms_per_step", C.c_double * MD_BATCH_TUNE_MAX),
+                ("cell_occupancy", C.c_double), ("trial_occupancy", C.c_double * MD_BATCH_TUNE_MAX)]
 
 
 def dptr(a: np.ndarray):

@@ -68,7 +68,7 @@ class Batch:
 
     def __init__(self, boxes: Sequence[Box], rc: float, precision: str = "mixed", skin: float = -1.0,
                  threads_per_molecule: int = 0, epsilon: float = 1.0, sigma: float = 1.0, mass: float = 1.0,
-                 shifted: bool = False, device: int = 0):
+                 shifted: bool = False, device: int = 0, cell_occupancy: float = 0.0):
         self.L = load_library()
         self.h = C.c_void_p()
         self.nbox = len(boxes)
@@ -83,6 +83,7 @@ class Batch:
         cfg.threads_per_molecule = threads_per_molecule
         cfg.skin = skin
         cfg.device = device
+        cfg.cell_occupancy = cell_occupancy
         rc_ = self.L.md_batch_create(C.byref(self.h), C.byref(cfg))
         if rc_ != abi.MD_OK:
             msg = self.L.md_batch_last_error(self.h).decode() if self.h.value else ""
@@ -140,9 +141,10 @@ class Batch:
     def autotune(self, dt: float, trial_steps: int = 30) -> dict:
         t = abi.MdBatchTuning()
         self._check(self.L.md_batch_autotune(self.h, dt, trial_steps, C.byref(t)), "md_batch_autotune")
-        trials = [(t.trial_skin[k], t.trial_tpm[k], t.trial_ms_per_step[k]) for k in range(t.ntrials)]
-        return {"skin": t.skin, "threads_per_molecule": t.threads_per_molecule, "ms_per_step": t.ms_per_step,
-                "trials": trials}
+        trials = [(t.trial_skin[k], t.trial_tpm[k], t.trial_occupancy[k], t.trial_ms_per_step[k])
+                  for k in range(t.ntrials)]
+        return {"skin": t.skin, "threads_per_molecule": t.threads_per_molecule, "cell_occupancy": t.cell_occupancy,
+                "ms_per_step": t.ms_per_step, "trials": trials}
 
     def stream(self) -> int:
         s = C.c_void_p()

@@ -68,9 +68,11 @@ def test_batch_struct_layouts_match_header():
 #include <stddef.h>
 #include "ls1gb300.h"
 int main(void) {
-  printf("%zu %zu %zu\n", sizeof(md_batch_config), sizeof(md_box_sums), sizeof(md_batch_tuning));
-  printf("%zu %zu %zu %zu\n", offsetof(md_batch_config, box_len), offsetof(md_batch_config, skin),
-         offsetof(md_batch_config, device), offsetof(md_batch_tuning, trial_ms_per_step));
+  printf("%zu %zu %zu %zu %zu\n", sizeof(md_batch_config), sizeof(md_box_sums), sizeof(md_batch_tuning),
+         sizeof(md_kernel_times), offsetof(md_kernel_times, adjoint_ms));
+  printf("%zu %zu %zu %zu %zu %zu\n", offsetof(md_batch_config, box_len), offsetof(md_batch_config, skin),
+         offsetof(md_batch_config, device), offsetof(md_batch_tuning, trial_ms_per_step),
+         offsetof(md_batch_config, cell_occupancy), offsetof(md_batch_tuning, trial_occupancy));
   return 0;
 }
 '''
@@ -82,8 +84,10 @@ int main(void) {
     out = [int(x) for x in subprocess.run([os.path.join(d, "t")], capture_output=True, text=True,
                                           check=True).stdout.split()]
     assert out[:3] == [ctypes.sizeof(t) for t in (abi.MdBatchConfig, abi.MdBoxSums, abi.MdBatchTuning)]
-    assert out[3:] == [abi.MdBatchConfig.box_len.offset, abi.MdBatchConfig.skin.offset,
-                       abi.MdBatchConfig.device.offset, abi.MdBatchTuning.trial_ms_per_step.offset]
+    assert out[3:5] == [ctypes.sizeof(abi.MdKernelTimes), abi.MdKernelTimes.adjoint_ms.offset]
+    assert out[5:] == [abi.MdBatchConfig.box_len.offset, abi.MdBatchConfig.skin.offset,
+                       abi.MdBatchConfig.device.offset, abi.MdBatchTuning.trial_ms_per_step.offset,
+                       abi.MdBatchConfig.cell_occupancy.offset, abi.MdBatchTuning.trial_occupancy.offset]
 
 
 def test_batch_create_without_gpu_fails_cleanly(lib):

@@ -135,6 +135,26 @@ def test_mixed_precision_adjoint_close_to_fp64(E):
     assert np.sqrt(((gr32 - gr64) ** 2).mean()) <= 2e-4 * np.sqrt((gr64 ** 2).mean())
 
 
+@pytest.mark.parametrize("shifted", [False, True])
+def test_mixed_single_component_lj_adjoint_close_to_fp64(E, shifted):
+    """The FP32 single-component LJ adjoint (with the pair Hessian-vector
+    product) against the FP64 adjoint on the same state."""
+    ps = psm.lj_fcc(6, 0.7, 1.1, seed=8, shifted=shifted, rc=2.5)
+    rng = np.random.default_rng(8)
+    ps.r = ps.r + rng.uniform(-0.15, 0.15, ps.r.shape)
+    gF = rng.normal(size=(ps.n, 3))
+    out = {}
+    for prec in ("fp64", "mixed"):
+        e = E.Engine(ps, 2.5, precision=prec, skin=0.3)
+        e.forces()
+        out[prec] = e.adjoint(0.7, -0.3, gF)
+        e.close()
+    gr64, gp64 = out["fp64"]
+    gr32, gp32 = out["mixed"]
+    assert np.abs(gp32 - gp64).max() <= 2e-4 * np.abs(gp64).max()
+    assert np.sqrt(((gr32 - gr64) ** 2).mean()) <= 2e-4 * np.sqrt((gr64 ** 2).mean())
+
+
 def test_lj_against_fp64_all_pairs_torch_reference(E):
     """N=2048 subset: FP64 all-pairs minimum-image LJ in torch (autograd)
     gives dU/dr, dU/deps, dU/dsigma and the virial's parameter gradients."""

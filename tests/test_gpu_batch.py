@@ -141,15 +141,20 @@ def test_batch_box_against_oracle(mods, boxes):
 def test_autotune_picks_a_measured_configuration(mods, boxes):
     _, B = mods
     bt = B.Batch(boxes, RC, precision="mixed")
-    bt.forces()
+    s0 = bt.forces()
     before = bt.molecules()
     t = bt.autotune(0.002, trial_steps=8)
     after = bt.molecules()
+    # the tuned configuration evaluates the same state to the same sums
+    s1 = bt.forces()
+    assert np.array_equal(s0[:, 2], s1[:, 2])
+    assert np.allclose(s1[:, 0], s0[:, 0], rtol=1e-6, atol=0)
     assert t["trials"], t
-    assert min(ms for _, _, ms in t["trials"]) == pytest.approx(t["ms_per_step"])
-    assert (t["skin"], t["threads_per_molecule"]) in [(s, p) for s, p, _ in t["trials"]]
+    assert min(ms for _, _, _, ms in t["trials"]) == pytest.approx(t["ms_per_step"])
+    assert (t["skin"], t["threads_per_molecule"], t["cell_occupancy"]) in [(s, p, o) for s, p, o, _ in t["trials"]]
     # the state is restored after the trials
     assert np.array_equal(before["r"], after["r"]) and np.array_equal(before["v"], after["v"])
     rec = bt.run(0.002, 20, graph_steps=10)
     assert np.all(np.isfinite(rec))
+    assert np.all(rec[:, :, 2] > 0)  # every box's sum m v^2 is recorded every step
     bt.close()
