@@ -516,17 +516,23 @@ def main():
         ids, comp, r, v, q, Lm = E.abi.molecule_arrays(ps)
         t0 = time.perf_counter()
         eng2 = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local)
+        t_up = time.perf_counter()
         eng2.forces()
+        t_f = time.perf_counter()
         rec = eng2.run(dt, a.steps, record=True)
+        t_run = time.perf_counter()
         out = eng2.molecules()
         t1 = time.perf_counter()
         e2e_s = max_over_ranks(pg, t1 - t0)
         eng2.close()
+        phases = {"create_upload_s": t_up - t0, "first_forces_s": t_f - t_up, "steps_s": t_run - t_f,
+                  "download_s": t1 - t_run}
         h2d = sum(x.nbytes for x in (ids, comp, r, v, q, Lm))
         d2h = sum(out[k].nbytes for k in out) + rec.nbytes
         e2e = {"value": world * n * a.steps / e2e_s, "unit": "molecule-updates/s",
                "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps,
-               "scope": "md_create + upload + first forces + K steps (per-step sums read back) + download"}
+               "scope": "md_create + upload + first forces + K steps (per-step sums read back) + download",
+               "phases": phases}
 
     cb = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:

@@ -192,6 +192,30 @@ int md_adjoint(md_ctx* ctx, double gU, double gW, const double* gF, double* grad
 int md_forces_lj_noalloc(const double* d_r, int64_t n, const double box[3], double rc, double eps, double sigma,
                          double shift6, double* d_F, double* d_upot_virial, void* stream);
 
+/* Homogeneous long-range correction (longRange/Homogeneous.cpp:22-146,
+ * Homogeneous::init + calculateLongRange): UpotCorr and VirialCorr of the
+ * current molecule counts, box volume, cut-offs and reaction field (what the
+ * reference adds to the global Upot and virial in
+ * Domain::calculateGlobalValues).  With add_to_molecule_virial != 0 it also
+ * adds VirialCorr / (3 N) to every molecule's virial tensor diagonal, as the
+ * reference does after each force evaluation.  MD_ERR_ARG when rc_lj does not
+ * exceed the sum of two LJ centres' distances from their molecule centres. */
+int md_longrange_homogeneous(md_ctx* ctx, int32_t add_to_molecule_virial, double* upot_corr, double* virial_corr);
+
+/* Global velocity-scaling thermostat (the reference's VELSCALE_THERMOSTAT with
+ * one thermostat: Domain::calculateGlobalValues, Domain.cpp:212-345, and
+ * VelocityScalingThermostat::apply, VelocityScalingThermostat.cpp:67-96):
+ * after the global sums of a step, beta_trans = (3 N T / sum m v^2)^0.4 and
+ * beta_rot = (rotDOF T / sum I w^2)^0.4 scale v and the angular momenta, with
+ * the reference's explosion heuristic when a beta falls below 0.9 (if
+ * explosion_heuristics != 0).  md_set_thermostat: target <= 0 switches it off
+ * (NVE) and resets the heuristic's counters; md_run then applies it every
+ * step on the device.  md_apply_thermostat: one application after
+ * md_integrate_post (the step-by-step path of the ls1 drop-in); returns the
+ * betas. */
+int md_set_thermostat(md_ctx* ctx, double target_temperature, int32_t explosion_heuristics);
+int md_apply_thermostat(md_ctx* ctx, double* beta_trans, double* beta_rot);
+
 /* Wait for all work of the context. */
 int md_sync(md_ctx* ctx);
 

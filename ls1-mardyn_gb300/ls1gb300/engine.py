@@ -62,6 +62,9 @@ def load_library(path: str = LIB_PATH):
     L.md_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.md_adjoint.argtypes = [vp, d, d, vp, vp, vp, i32]
     L.md_time_kernels.argtypes = [vp, i32, C.POINTER(abi.MdKernelTimes)]
+    L.md_longrange_homogeneous.argtypes = [vp, i32, dp, dp]
+    L.md_set_thermostat.argtypes = [vp, d, i32]
+    L.md_apply_thermostat.argtypes = [vp, dp, dp]
     L.md_batch_create.argtypes = [C.POINTER(vp), C.POINTER(abi.MdBatchConfig)]
     L.md_batch_destroy.argtypes = [vp]
     L.md_batch_last_error.argtypes = [vp]
@@ -174,6 +177,24 @@ class Engine:
         self._check(self.L.md_adjoint(self.h, float(gU), float(gW), None if gFa is None else gFa.ctypes.data,
                                       gr.ctypes.data, gp.ctypes.data, npar), "md_adjoint")
         return gr, gp[:npar]
+
+    def set_thermostat(self, target_temperature: float, explosion_heuristics: bool = True):
+        """Global velocity-scaling thermostat at the target (<= 0: NVE), applied by run()."""
+        self._check(self.L.md_set_thermostat(self.h, float(target_temperature), int(explosion_heuristics)),
+                    "md_set_thermostat")
+
+    def apply_thermostat(self):
+        """One thermostat application after post(); returns (beta_trans, beta_rot)."""
+        bt, br = C.c_double(), C.c_double()
+        self._check(self.L.md_apply_thermostat(self.h, C.byref(bt), C.byref(br)), "md_apply_thermostat")
+        return bt.value, br.value
+
+    def longrange_homogeneous(self, add_to_molecule_virial: bool = False):
+        """(UpotCorr, VirialCorr) of the homogeneous long-range correction."""
+        u, w = C.c_double(), C.c_double()
+        self._check(self.L.md_longrange_homogeneous(self.h, int(add_to_molecule_virial), C.byref(u), C.byref(w)),
+                    "md_longrange_homogeneous")
+        return u.value, w.value
 
     def molecules(self) -> dict:
         n = self.n

@@ -52,6 +52,10 @@ struct orc_sys {
     /* cells */
     int64_t ncells;
     int64_t *cstart, *clist, *mcell;
+    /* global velocity-scaling thermostat (target <= 0: NVE) and the explosion
+       heuristic's counters (Domain.cpp:74-76) */
+    double thermo_T;
+    int thermo_heur, th_counter, th_warning, th_error;
 };
 
 static int g_threads = 1;
@@ -1080,7 +1084,79 @@ int orc_post(orc_sys* s, double dt, md_kinetic_out* out) {
     return MD_OK;
 }
 
-/* Simulation::simulateOneTimestep hot part for NVE (Simulation.cpp:1076-1300) */
+int orc_set_thermostat(orc_sys* s, double target_temperature, int32_t explosion_heuristics) {
+    s->thermo_T = target_temperature;
+    s->thermo_heur = explosion_heuristics != 0;
+    s->th_counter = s->th_warning = s->th_error = 0;
+    return MD_OK;
+}
+
+/* One global thermostat: Domain::calculateGlobalValues (Domain.cpp:212-345;
+ * beta_trans = (3 N T / sum m v^2)^0.4, beta_rot = (rotDOF T / sum I w^2)^0.4,
+ * and the explosion heuristic: when a beta falls below MIN_BETA = 0.9,
+ * molecules above 10 T of translational (3 rotDOF T of rotational) kinetic
+ * energy are slowed down to it, the betas become 1 and beta_rot^0.0091, and
+ * the counters advance), then VelocityScalingThermostat::apply
+ * (VelocityScalingThermostat.cpp:67-96): v *= beta_trans, D *= beta_rot. */
+int orc_thermostat(orc_sys* s, const md_kinetic_out* ko, double* beta_trans, double* beta_rot) {
+    const double Ti = s->thermo_T;
+    const unsigned long N = (unsigned long)ko->n, rotDOF = (unsigned long)ko->rot_dof;
+    const double summv2 = ko->summv2, sumIw2 = rotDOF > 0 ? ko->sumIw2 : 0.0;
+    double bt = 1.0, br = 1.0;
+    if (Ti > 0.0 && N > 0) {
+        bt = pow(3.0 * N * Ti / summv2, 0.4);
+        br = sumIw2 == 0.0 ? 1.0 : pow(rotDOF * Ti / sumIw2, 0.4);
+    }
+    if ((bt < 0.9 || br < 0.9) && 0 >= s->th_error && s->thermo_heur) {
+        const double limit_energy = 10.0 * Ti;
+        for (int64_t k = 0; k < s->n; ++k) {
+            const ocomp* C = &s->cdef[s->mcomp[k]];
+            double* v = s->v + 3 * k;
+            const double ut = 0.5 * C->m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            if (ut > limit_energy) {
+                const double c = sqrt(limit_energy / ut);
+                for (int d = 0; d < 3; ++d) { v[d] *= c; s->F[3 * k + d] *= c; }
+            }
+            if (C->rot_dof > 0) {
+                const double limit_rot = 3.0 * C->rot_dof * Ti;
+                double w[3];
+                q_rotateinv(s->q + 4 * k, s->L + 3 * k, w);
+                double Iw2 = 0.;
+                for (int d = 0; d < 3; ++d) {
+                    w[d] *= C->invI[d];
+                    Iw2 += C->I[d] * w[d] * w[d];
+                }
+                const double ur = 0.5 * Iw2;
+                if (ur > limit_rot) {
+                    const double c = sqrt(limit_rot / ur);
+                    for (int d = 0; d < 3; ++d) { s->L[3 * k + d] *= c; s->M[3 * k + d] *= c; }
+                }
+            }
+        }
+        const int since = 4000 - s->th_counter;
+        if (since >= 40) {
+            if (s->th_warning > 0) s->th_error = s->th_warning;
+            if (s->th_counter > 0) s->th_warning = s->th_counter;
+            s->th_counter = 4000;
+        }
+        bt = 1.0;
+        br = pow(br, 0.0091);
+    }
+    if (s->th_counter > 0) s->th_counter--;
+    if (s->th_warning > 0) s->th_warning--;
+    if (s->th_error > 0) s->th_error--;
+    for (int64_t k = 0; k < s->n; ++k)
+        for (int d = 0; d < 3; ++d) {
+            s->v[3 * k + d] *= bt;
+            s->L[3 * k + d] *= br;
+        }
+    if (beta_trans) *beta_trans = bt;
+    if (beta_rot) *beta_rot = br;
+    return MD_OK;
+}
+
+/* Simulation::simulateOneTimestep hot part (Simulation.cpp:1076-1300): NVE, or
+ * with the global velocity-scaling thermostat after the global values. */
 int orc_run(orc_sys* s, double dt, int32_t nsteps, md_step_record* rec) {
     for (int32_t k = 0; k < nsteps; ++k) {
         orc_pre(s, dt);
@@ -1096,6 +1172,103 @@ int orc_run(orc_sys* s, double dt, int32_t nsteps, md_step_record* rec) {
             rec[k].summv2 = ko.summv2;
             rec[k].sumIw2 = ko.rot_dof > 0 ? ko.sumIw2 : 0.0;
         }
+        if (s->thermo_T > 0.0) orc_thermostat(s, &ko, NULL, NULL);
     }
+    return MD_OK;
+}
+
+/* ---------------------------------------------------------------- long range
+ * Homogeneous::init + calculateLongRange (src/longRange/Homogeneous.cpp:22-146)
+ * with its tail integrals (Homogeneous.cpp:158-196): for every pair of LJ
+ * centres whose shift6 is zero, the integral of the LJ potential (virial)
+ * beyond rcLJ over a uniform fluid, in the form for two centred sites, one
+ * centred and one off-centre site (distance tau from its molecule's centre),
+ * or two off-centre sites; weighted with N_i N_j eps24 and scaled by
+ * pi rho / (3 N).  Plus the reaction-field self term of each component's net
+ * dipole (sum of q r over its charges and of the unit-normalised point
+ * dipoles), -1/2 epsRFInvrc3 sum_i N_i |mu_i|^2, counted once in Upot and
+ * three times in the virial.  The operation order is the reference's. */
+static double tl_cc_u(int n, double rc, double s2) {
+    return -pow(rc, 2 * n + 3) / (pow(s2, n) * (2 * n + 3));
+}
+static double tl_cs_u(int n, double rc, double s2, double t) {
+    return -(pow(rc + t, 2 * n + 3) - pow(rc - t, 2 * n + 3)) * rc / (4 * pow(s2, n) * t * (n + 1) * (2 * n + 3)) +
+           (pow(rc + t, 2 * n + 4) - pow(rc - t, 2 * n + 4)) / (4 * pow(s2, n) * t * (n + 1) * (2 * n + 3) * (2 * n + 4));
+}
+static double tl_ss_u(int n, double rc, double s2, double t1, double t2) {
+    double tp = t1 + t2, tm = t1 - t2;
+    return -(pow(rc + tp, 2 * n + 4) - pow(rc + tm, 2 * n + 4) - pow(rc - tm, 2 * n + 4) + pow(rc - tp, 2 * n + 4)) *
+               rc / (8 * pow(s2, n) * t1 * t2 * (n + 1) * (2 * n + 3) * (2 * n + 4)) +
+           (pow(rc + tp, 2 * n + 5) - pow(rc + tm, 2 * n + 5) - pow(rc - tm, 2 * n + 5) + pow(rc - tp, 2 * n + 5)) /
+               (8 * pow(s2, n) * t1 * t2 * (n + 1) * (2 * n + 3) * (2 * n + 4) * (2 * n + 5));
+}
+static double tl_cc_v(int n, double rc, double s2) { return 2 * n * tl_cc_u(n, rc, s2); }
+static double tl_cs_v(int n, double rc, double s2, double t) {
+    return -(pow(rc + t, 2 * n + 2) - pow(rc - t, 2 * n + 2)) * rc * rc / (4 * pow(s2, n) * t * (n + 1)) -
+           3 * tl_cs_u(n, rc, s2, t);
+}
+static double tl_ss_v(int n, double rc, double s2, double t1, double t2) {
+    double tp = t1 + t2, tm = t1 - t2;
+    return -(pow(rc + tp, 2 * n + 3) - pow(rc + tm, 2 * n + 3) - pow(rc - tm, 2 * n + 3) + pow(rc - tp, 2 * n + 3)) *
+               rc * rc / (8 * pow(s2, n) * t1 * t2 * (n + 1) * (2 * n + 3)) -
+           3 * tl_ss_u(n, rc, s2, t1, t2);
+}
+
+int orc_longrange_homogeneous(const orc_sys* s, double* upot_corr, double* virial_corr) {
+    const double rclj = s->cfg.rc_lj, rc = s->cfg.rc;
+    double cnt[MAXC] = {0};
+    for (int64_t k = 0; k < s->n; ++k) cnt[s->mcomp[k]] += 1.0;
+    double U = 0.0, W = 0.0, self = 0.0;
+    unsigned long nmol = 0;
+    for (int i = 0; i < s->ncomp; ++i) {
+        const ocomp* ci = &s->cdef[i];
+        nmol += (unsigned long)cnt[i];
+        double bal[3] = {0, 0, 0};
+        for (int k = 0; k < ci->nch; ++k)
+            for (int d = 0; d < 3; ++d) bal[d] += ci->ch[k][4] * ci->ch[k][d];
+        for (int k = 0; k < ci->ndi; ++k) {
+            double ee = 0;
+            for (int d = 0; d < 3; ++d) ee += ci->di[k][3 + d] * ci->di[k][3 + d];
+            double inv = 1.0 / sqrt(ee);
+            for (int d = 0; d < 3; ++d) bal[d] += ci->di[k][6] * ci->di[k][3 + d] * inv;
+        }
+        double my2 = 0.0;
+        for (int d = 0; d < 3; ++d) my2 += bal[d] * bal[d];
+        self += my2 * cnt[i];
+        for (int j = 0; j < s->ncomp; ++j) {
+            const ocomp* cj = &s->cdef[j];
+            for (int a = 0; a < ci->nlj; ++a) {
+                double t1 = sqrt(ci->lj[a][0] * ci->lj[a][0] + ci->lj[a][1] * ci->lj[a][1] + ci->lj[a][2] * ci->lj[a][2]);
+                for (int b = 0; b < cj->nlj; ++b) {
+                    double t2 = sqrt(cj->lj[b][0] * cj->lj[b][0] + cj->lj[b][1] * cj->lj[b][1] +
+                                     cj->lj[b][2] * cj->lj[b][2]);
+                    if (t1 + t2 >= rclj) return MD_ERR_ARG;  /* cut-off too small for the correction */
+                    const int g = (ci->ljoff + a) * s->nlj + cj->ljoff + b;
+                    if (s->shift6[g] != 0.0) continue;
+                    double fac = cnt[i] * cnt[j] * s->eps24[g], s2 = s->sig2[g];
+                    if (t1 == 0. && t2 == 0.) {
+                        U += fac * (tl_cc_u(-6, rclj, s2) - tl_cc_u(-3, rclj, s2));
+                        W += fac * (tl_cc_v(-6, rclj, s2) - tl_cc_v(-3, rclj, s2));
+                    } else if (t1 != 0. && t2 != 0.) {
+                        U += fac * (tl_ss_u(-6, rclj, s2, t1, t2) - tl_ss_u(-3, rclj, s2, t1, t2));
+                        W += fac * (tl_ss_v(-6, rclj, s2, t1, t2) - tl_ss_v(-3, rclj, s2, t1, t2));
+                    } else {
+                        double t = t2 == 0. ? t1 : t2;
+                        U += fac * (tl_cs_u(-6, rclj, s2, t) - tl_cs_u(-3, rclj, s2, t));
+                        W += fac * (tl_cs_v(-6, rclj, s2, t) - tl_cs_v(-3, rclj, s2, t));
+                    }
+                }
+            }
+        }
+    }
+    const double vol = (s->cfg.box_max[0] - s->cfg.box_min[0]) * (s->cfg.box_max[1] - s->cfg.box_min[1]) *
+                       (s->cfg.box_max[2] - s->cfg.box_min[2]);
+    const double rho = (double)nmol / vol;
+    const double pi = 3.14159265358979323846;  /* M_PI */
+    const double fac = pi * rho / (3. * (double)nmol);
+    const double epsRFInvrc3 = 2. * (s->cfg.eps_rf - 1.) / ((rc * rc * rc) * (2. * s->cfg.eps_rf + 1.));
+    const double selfterm = -0.5 * epsRFInvrc3 * self;
+    *upot_corr = fac * U + selfterm;
+    *virial_corr = -fac * W + 3. * selfterm;
     return MD_OK;
 }

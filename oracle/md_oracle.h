@@ -40,6 +40,11 @@ int orc_forces(orc_sys* s, md_forces_out* out, double* kernel_calls);
 int orc_pre(orc_sys* s, double dt);
 int orc_post(orc_sys* s, double dt, md_kinetic_out* out);
 int orc_run(orc_sys* s, double dt, int32_t nsteps, md_step_record* rec);
+/* global velocity-scaling thermostat (target <= 0: NVE), applied by orc_run */
+int orc_set_thermostat(orc_sys* s, double target_temperature, int32_t explosion_heuristics);
+int orc_thermostat(orc_sys* s, const md_kinetic_out* ko, double* beta_trans, double* beta_rot);
+/* Homogeneous long-range correction (longRange/Homogeneous.cpp:22-146) */
+int orc_longrange_homogeneous(const orc_sys* s, double* upot_corr, double* virial_corr);
 
 #ifdef __cplusplus
 }

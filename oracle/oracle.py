@@ -50,6 +50,8 @@ def lib():
         L.orc_pre.argtypes = [vp, C.c_double]
         L.orc_post.argtypes = [vp, C.c_double, C.POINTER(abi.MdKineticOut)]
         L.orc_run.argtypes = [vp, C.c_double, i32, C.POINTER(abi.MdStepRecord)]
+        L.orc_longrange_homogeneous.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_set_thermostat.argtypes = [vp, C.c_double, i32]
         _lib = L
     return _lib
 
@@ -106,6 +108,17 @@ class Oracle:
         ko = abi.MdKineticOut()
         lib().orc_post(self.h, dt, C.byref(ko))
         return ko
+
+    def set_thermostat(self, target_temperature, explosion_heuristics=True):
+        lib().orc_set_thermostat(self.h, target_temperature, int(explosion_heuristics))
+
+    def longrange_homogeneous(self):
+        """(UpotCorr, VirialCorr) of the homogeneous long-range correction."""
+        u, w = C.c_double(), C.c_double()
+        rc = lib().orc_longrange_homogeneous(self.h, C.byref(u), C.byref(w))
+        if rc:
+            raise RuntimeError(f"orc_longrange_homogeneous: {rc}")
+        return u.value, w.value
 
     def run(self, dt, nsteps):
         rec = (abi.MdStepRecord * max(nsteps, 1))()

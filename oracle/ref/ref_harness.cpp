@@ -11,6 +11,16 @@
 //       run the serial periodic exchange (leaving particles + halo copies),
 //       build the SoA caches, traverse with VectorizedCellProcessor and call
 //       calcFM on every inner molecule.  Also traverses with the FlopCounter.
+//   nvt <file.inp> <rc> <rcLJ> <dt> <nsteps> <T>
+//       As `steps`, with the global velocity-scaling thermostat at target T:
+//       after the global values of each step, v *= beta_trans and
+//       D *= beta_rot (Simulation::simulateOneTimestep, VELSCALE_THERMOSTAT
+//       with one thermostat).  STEP records carry the values before scaling
+//       and a BETA record follows each.
+//   lrc <file.inp> <rc> <rcLJ>
+//       The homogeneous long-range correction (longRange/Homogeneous): init +
+//       calculateLongRange, then the global values with zero local Upot and
+//       virial, so the printed global Upot and virial are the corrections.
 //   steps <file.inp> <rc> <rcLJ> <dt> <nsteps>
 //       NVE Leapfrog steps with the periodic halo, in the order of the
 //       reference's Simulation::simulateOneTimestep (thermostat off, no
@@ -23,6 +33,8 @@
 //   UPOT <local Upot>   VIRIAL <local virial>
 //   COUNTS <molecule distances> {<kernel calls> <macro calls>} x 7 potentials
 //   STEP <k> <Upot> <virial> <summv2> <sumIw2>
+//   LRC <UpotCorr> <VirialCorr>
+//   BETA <k> <beta_trans> <beta_rot>
 //   MOL <id> <comp> <cell> r[3] v[3] q[4] L[3] F[3] M[3] Vi[3]
 
 #include <cstdio>
@@ -33,11 +45,46 @@
 #include <iostream>
 #include <memory>
 
-#include "Domain.h"
+// Simulation's particle-container pointer is private; the long-range mode
+// points it at the harness's LinkedCells (the reference's Domain fetches the
+// molecule count through it).  Standard headers are included first so that
+// only the reference's own classes are opened.
+#include <any>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <fstream>
+#include <functional>
+#include <list>
+#include <map>
+#include <optional>
+#include <random>
+#include <set>
+#include <sstream>
+#include <stack>
+#include <tuple>
+#include <unordered_map>
+#include <utility>
+#include <variant>
+#include <iomanip>
+#include <mutex>
+#include <thread>
+#include <limits>
+#include <numeric>
+#include <bitset>
+#include <deque>
+#include <queue>
+#include <cstring>
+#include <omp.h>
+#define private public
 #include "Simulation.h"
+#undef private
+#include "Domain.h"
 #include "ensemble/EnsembleBase.h"
 #include "integrators/Leapfrog.h"
 #include "io/ASCIIReader.h"
+#include "longRange/Homogeneous.h"
+#include "thermostats/VelocityScalingThermostat.h"
 #include "molecules/Molecule.h"
 #include "parallel/DomainDecompBase.h"
 #include "particleContainer/LinkedCells.h"
@@ -150,10 +197,16 @@ void forceStep(Setup& s, VectorizedCellProcessor& vcp) {
 	s.lc->deleteOuterParticles();
 }
 
-int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nsteps) {
+int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nsteps, double T = 0.0) {
 	Setup s;
 	load(s, file, rc, rcLJ);
-	s.domain->thermostatOff();
+	if (T > 0.0) {
+		s.domain->thermostatOn();
+		s.domain->setGlobalTemperature(T);
+	} else {
+		s.domain->thermostatOff();
+	}
+	VelocityScalingThermostat thermostat;
 	s.dd->exchangeMolecules(s.lc, s.domain);
 	s.lc->updateMoleculeCaches();
 	s.domain->initParameterStreams(rc, rcLJ);
@@ -176,8 +229,31 @@ int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nst
 		s.domain->calculateGlobalValues(s.dd, s.lc, false, 1.0);
 		std::printf("STEP %d %.17g %.17g %.17g %.17g\n", k, upot, vir,
 					2.0 * s.domain->getGlobalUkinTrans(), 2.0 * s.domain->getGlobalUkinRot());
+		if (T > 0.0) {
+			thermostat.setGlobalBetaTrans(s.domain->getGlobalBetaTrans());
+			thermostat.setGlobalBetaRot(s.domain->getGlobalBetaRot());
+			thermostat.apply(s.lc);
+			std::printf("BETA %d %.17g %.17g\n", k, s.domain->getGlobalBetaTrans(), s.domain->getGlobalBetaRot());
+		}
 	}
 	printMolecules(s);
+	return 0;
+}
+
+int runLrc(const std::string& file, double rc, double rcLJ) {
+	Setup s;
+	load(s, file, rc, rcLJ);
+	s.domain->thermostatOff();
+	s.domain->initParameterStreams(rc, rcLJ);
+	global_simulation->_moleculeContainer = s.lc;
+	Homogeneous lrc(rc, rcLJ, s.domain, s.lc, global_simulation);
+	lrc.init();
+	lrc.calculateLongRange();
+	s.domain->setLocalUpot(0.0);
+	s.domain->setLocalVirial(0.0);
+	s.domain->calculateGlobalValues(s.dd, s.lc, false, 1.0);
+	const double n = (double)s.domain->getglobalNumMolecules(false);
+	std::printf("LRC %.17g %.17g\n", s.domain->getGlobalUpot(), s.domain->getAverageGlobalVirial() * n);
 	return 0;
 }
 
@@ -189,8 +265,13 @@ int main(int argc, char** argv) {
 	Log::global_log = std::make_unique<Log::Logger>(Log::Warning, std::shared_ptr<std::ostream>(&std::cerr, [](void*) {}));
 	if (argc >= 6 && std::string(argv[1]) == "forces")
 		return runForces(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atoi(argv[5]) != 0);
+	if (argc >= 8 && std::string(argv[1]) == "nvt")
+		return runSteps(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]),
+						std::atof(argv[7]));
+	if (argc >= 5 && std::string(argv[1]) == "lrc")
+		return runLrc(argv[2], std::atof(argv[3]), std::atof(argv[4]));
 	if (argc >= 7 && std::string(argv[1]) == "steps")
 		return runSteps(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]));
-	std::fprintf(stderr, "usage: %s forces <inp> <rc> <rcLJ> <periodic> | steps <inp> <rc> <rcLJ> <dt> <n>\n", argv[0]);
+	std::fprintf(stderr, "usage: %s forces <inp> <rc> <rcLJ> <periodic> | lrc <inp> <rc> <rcLJ> | steps <inp> <rc> <rcLJ> <dt> <n> | nvt <inp> <rc> <rcLJ> <dt> <n> <T>\n", argv[0]);
 	return 2;
 }

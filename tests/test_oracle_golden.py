@@ -105,3 +105,32 @@ def test_oracle_thread_count_independent():
     for F, u in res[1:]:
         assert np.array_equal(F, res[0][0])
         assert abs(u - res[0][1]) <= 1e-12 * abs(res[0][1])
+
+
+@pytest.mark.parametrize("name", golden_io.names("lrc_"))
+def test_oracle_longrange_homogeneous_matches_reference(name):
+    """Homogeneous long-range correction (UpotCorr, VirialCorr) equal to the
+    reference's own, bit for bit."""
+    ps, g = golden_io.load(name)
+    o = Oracle(ps, g["rc"], g["rc_lj"])
+    u, w = o.longrange_homogeneous()
+    assert u == float(g["upot_corr"]) and w == float(g["virial_corr"])
+
+
+@pytest.mark.parametrize("name", golden_io.names("nvtt_"))
+def test_oracle_velocity_scaling_thermostat_matches_reference(name):
+    """NVT runs with the reference's global velocity-scaling thermostat."""
+    ps, g = golden_io.load(name)
+    o = Oracle(ps, g["rc"], g["rc_lj"], (1, 1, 1), threads=8)
+    o.set_thermostat(float(g["target_temperature"]))
+    o.rebin()
+    o.forces()
+    rec = o.run(float(g["dt"]), int(g["nsteps"]))
+    ref = g["steps"][1:, 1:]
+    for col in range(4):
+        scale = max(np.abs(ref[:, col]).max(), 1e-300)
+        assert np.abs(rec[:, col] - ref[:, col]).max() <= 1e-10 * scale, col
+    m = o.molecules()
+    a, b = _by_id(m["ids"]), _by_id(g["out_ids"])
+    for key, gk in (("r", "out_r"), ("v", "out_v"), ("q", "out_q"), ("L", "out_L")):
+        assert np.abs(m[key][a] - g[gk][b]).max() < 1e-9, key
