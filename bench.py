@@ -64,10 +64,10 @@ BATCH_DESC = ("512 independent periodic 1CLJ boxes, N log-uniform in [500, 20000
               "T* U[0.7, 1.3], rc=2.5, dt=0.002, graphs of 100 steps, skin and threads per molecule row autotuned")
 DEFAULT_SKIN = {"lj4m": 0.25, "lj1m": 0.25, "lj32k": 0.3, "slab": 0.25, "mix1m": 0.1}
 FLOP_PER_PAIR_LJ = 39.0  # reference FlopCounter model: 31 per LJ site pair + 8 per molecule distance
-# DRAM bytes (read + write) of one k_force_lj32 launch per pair-candidate list entry, from an ncu
-# capture of the 1,000,188-molecule case (467.0 MB for 87.17 entries per molecule); traffic grows
+# DRAM bytes (read + write) of one k_force_lj32x2 launch per pair-candidate list entry, from an ncu
+# capture of the 1,000,188-molecule case (598.9 MB for 100.2 entries per molecule); traffic grows
 # with the entries read, so it is scaled by the live entry count.
-FORCE_DRAM_BYTES_PER_ENTRY = 467.0e6 / (1_000_188 * 87.17)
+FORCE_DRAM_BYTES_PER_ENTRY = 598.9e6 / (1_000_188 * 100.2)
 
 
 # ---------------------------------------------------------------- CUDA events on the engine stream
@@ -547,7 +547,7 @@ def main():
             "config": {"workload": desc, "precision": a.precision, "skin": skin, "molecules": n,
                        "parallelism": f"replicas x{world}", "l2": "working set > L2 (GBs), no flush needed"},
             "gpu_launches": int(kt.launches_per_step * a.steps),
-            "roofline": {"bound": "hbm", "kernel": "k_force_lj32" if a.precision == "mixed" else "k_force_lj64",
+            "roofline": {"bound": "hbm", "kernel": "k_force_lj32x2" if a.precision == "mixed" else "k_force_lj64",
                          "achieved": hbm_bytes / (kt.force_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                          "frac": hbm_bytes / (kt.force_ms * 1e-3) / 1e9 / hbm_peak,
                          "traffic": traffic, "peak_source": hbm_src,

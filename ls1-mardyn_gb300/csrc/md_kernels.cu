@@ -73,6 +73,21 @@ __device__ __forceinline__ void warp_partial(double* partials, int pstride, int 
         partials[(size_t)slot * pstride + ((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5)] = v;
 }
 
+// A slot this kernel contributes nothing to: lane 0 writes the zero partial
+// without a reduction.
+__device__ __forceinline__ void warp_partial_zero(double* partials, int pstride, int slot) {
+    if ((threadIdx.x & 31) == 0)
+        partials[(size_t)slot * pstride + ((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5)] = 0.0;
+}
+
+// Integer-valued partial (a pair count): reduced exactly in FP32 across the
+// warp (|sum| < 2^24), converted once.
+__device__ __forceinline__ void warp_partial_count(double* partials, int pstride, int slot, float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0)
+        partials[(size_t)slot * pstride + ((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5)] = (double)v;
+}
+
 // Sum `v` over the block (blockDim multiple of 32, <= 1024); result valid in thread 0.
 __device__ double block_sum(double v, double* sh) {
     v = warp_sum(v);
@@ -734,12 +749,12 @@ __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __
         S.Vx[i] = 0.5 * (double)vx; S.Vy[i] = 0.5 * (double)vy; S.Vz[i] = 0.5 * (double)vz;
     }
     warp_partial(partials, pstride, 0, (double)up);
-    warp_partial(partials, pstride, 1, 0.0);
+    warp_partial_zero(partials, pstride, 1);
     warp_partial(partials, pstride, 2, (double)vir);
-    warp_partial(partials, pstride, 3, 0.0);
-    warp_partial(partials, pstride, 4, (double)nmol);
-    warp_partial(partials, pstride, 5, (double)npairs);
-    for (int sl = 6; sl < 12; ++sl) warp_partial(partials, pstride, sl, 0.0);
+    warp_partial_zero(partials, pstride, 3);
+    warp_partial_count(partials, pstride, 4, (float)nmol);
+    warp_partial_count(partials, pstride, 5, (float)npairs);
+    for (int sl = 6; sl < 12; ++sl) warp_partial_zero(partials, pstride, sl);
 }
 
 // FP64 re-decision of a pair near a cut-off, always evaluated in the frame of
@@ -749,56 +764,13 @@ __device__ __forceinline__ double fp64_r2_canon(const State& S, int i, int j, ui
     return j > i ? fp64_r2(S, i, j, code) : fp64_r2(S, j, i, 26u - code);
 }
 
-// Candidate-row loads of the LJ kernels: the next 16-byte chunk of a row is
-// loaded one iteration ahead with an L2 prefetch-size hint of 256 bytes (rows
-// are read sequentially).  MD_LIST_LOAD_MODE 3 also marks the row data
-// evict-first in L2 (it is read once per launch), so that L2 keeps the
-// neighbour positions; MD_POS_HINT 1 marks the position gathers evict-last.
-#ifndef MD_LIST_LOAD_MODE
-#define MD_LIST_LOAD_MODE 1
-#endif
-#ifndef MD_POS_HINT
-#define MD_POS_HINT 0
-#endif
-__device__ __forceinline__ uint64_t l2_policy_first() {
-    uint64_t p = 0;
-#if MD_LIST_LOAD_MODE == 3
-    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-#endif
-    return p;
-}
-
-__device__ __forceinline__ uint64_t l2_policy_last() {
-    uint64_t p = 0;
-#if MD_POS_HINT == 1
-    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-#endif
-    return p;
-}
-
-__device__ __forceinline__ uint4 ld_row_chunk(const uint4* p, uint64_t pol) {
+// Candidate-row loads of the LJ kernels: rows are read sequentially, 16 bytes
+// at a time, with an L2 prefetch-size hint of 256 bytes; the kernels load the
+// next chunk one iteration ahead.
+__device__ __forceinline__ uint4 ld_row_chunk(const uint4* p) {
     uint4 r;
-#if MD_LIST_LOAD_MODE == 3
-    asm("ld.global.nc.L2::cache_hint.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
-        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p), "l"(pol));
-#else
-    (void)pol;
-    asm("ld.global.nc.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4];"
-        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
-#endif
+    asm("ld.global.nc.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
     return r;
-}
-
-__device__ __forceinline__ float4 ld_pos(const float4* p, uint64_t pol) {
-#if MD_POS_HINT == 1
-    float4 r;
-    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p), "l"(pol));
-    return r;
-#else
-    (void)pol;
-    return __ldg(p);
-#endif
 }
 
 __device__ __forceinline__ float rcp_approx(float x) {
@@ -913,9 +885,6 @@ __device__ __forceinline__ void lj_pack2(const float2 pix, const float2 piy, con
 // frame), so Upot, virial and the pair count are half the per-molecule
 // sums over all neighbours.  Force sums are Kahan-compensated per group of
 // four candidates; eps24 multiplies the sums once per molecule.
-#ifndef MD_LJ_GROUP
-#define MD_LJ_GROUP 4  // candidates per iteration of k_force_lj32x2 (4 or 8)
-#endif
 #ifndef MD_LJX2_MIN_BLOCKS
 #define MD_LJX2_MIN_BLOCKS 3  // blocks of 256 per SM the register budget is sized for
 #endif
@@ -948,46 +917,12 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
         AmbList am;
         am.n = 0;
         const uint4* row = reinterpret_cast<const uint4*>(nbr + (size_t)i * maxnb);
-        const uint64_t pol_row = l2_policy_first(), pol_pos = l2_policy_last();
-#if MD_LJ_GROUP == 8
-        // two chunks (eight candidates) per iteration; rows are padded to a multiple of eight
-        uint4 nx = cnt > 0 ? ld_row_chunk(row, pol_row) : make_uint4(0u, 0u, 0u, 0u);
-        uint4 ny = cnt > 4 ? ld_row_chunk(row + 1, pol_row) : make_uint4(0u, 0u, 0u, 0u);
-        for (int k = 0; k < cnt; k += 8) {
-            const uint4 e4 = nx, f4 = ny;
-            if (k + 8 < cnt) nx = ld_row_chunk(row + (k >> 2) + 2, pol_row);
-            if (k + 12 < cnt) ny = ld_row_chunk(row + (k >> 2) + 3, pol_row);
-            const bool two = k + 4 < cnt;
-            const float4 pa = ld_pos(&xlf[e4.x & MD_INDEX_MASK], pol_pos), pb = ld_pos(&xlf[e4.y & MD_INDEX_MASK], pol_pos);
-            const float4 pc = ld_pos(&xlf[e4.z & MD_INDEX_MASK], pol_pos), pd = ld_pos(&xlf[e4.w & MD_INDEX_MASK], pol_pos);
-            const uint4 g4 = f4;
-            float4 qa, qb, qc, qd;
-            if (two) {
-                qa = ld_pos(&xlf[g4.x & MD_INDEX_MASK], pol_pos); qb = ld_pos(&xlf[g4.y & MD_INDEX_MASK], pol_pos);
-                qc = ld_pos(&xlf[g4.z & MD_INDEX_MASK], pol_pos); qd = ld_pos(&xlf[g4.w & MD_INDEX_MASK], pol_pos);
-            }
-            a.gx = a.gy = a.gz = make_float2(0.f, 0.f);
-            lj_pack2(pix, piy, piz, pa, pb, nsoff[e4.x >> MD_CODE_SHIFT], nsoff[e4.y >> MD_CODE_SHIFT], e4.x, e4.y,
-                     ns2, rc2f, band, a, am);
-            lj_pack2(pix, piy, piz, pc, pd, nsoff[e4.z >> MD_CODE_SHIFT], nsoff[e4.w >> MD_CODE_SHIFT], e4.z, e4.w,
-                     ns2, rc2f, band, a, am);
-            if (two) {
-                lj_pack2(pix, piy, piz, qa, qb, nsoff[g4.x >> MD_CODE_SHIFT], nsoff[g4.y >> MD_CODE_SHIFT], g4.x,
-                         g4.y, ns2, rc2f, band, a, am);
-                lj_pack2(pix, piy, piz, qc, qd, nsoff[g4.z >> MD_CODE_SHIFT], nsoff[g4.w >> MD_CODE_SHIFT], g4.z,
-                         g4.w, ns2, rc2f, band, a, am);
-            }
-            fx.add(a.gx.x + a.gx.y);
-            fy.add(a.gy.x + a.gy.y);
-            fz.add(a.gz.x + a.gz.y);
-        }
-#else
-        uint4 nx = cnt > 0 ? ld_row_chunk(row, pol_row) : make_uint4(0u, 0u, 0u, 0u);
+        uint4 nx = cnt > 0 ? ld_row_chunk(row) : make_uint4(0u, 0u, 0u, 0u);
         for (int k = 0; k < cnt; k += 4) {
             const uint4 e4 = nx;
-            if (k + 4 < cnt) nx = ld_row_chunk(row + (k >> 2) + 1, pol_row);
-            const float4 pa = ld_pos(&xlf[e4.x & MD_INDEX_MASK], pol_pos), pb = ld_pos(&xlf[e4.y & MD_INDEX_MASK], pol_pos);
-            const float4 pc = ld_pos(&xlf[e4.z & MD_INDEX_MASK], pol_pos), pd = ld_pos(&xlf[e4.w & MD_INDEX_MASK], pol_pos);
+            if (k + 4 < cnt) nx = ld_row_chunk(row + (k >> 2) + 1);
+            const float4 pa = __ldg(&xlf[e4.x & MD_INDEX_MASK]), pb = __ldg(&xlf[e4.y & MD_INDEX_MASK]);
+            const float4 pc = __ldg(&xlf[e4.z & MD_INDEX_MASK]), pd = __ldg(&xlf[e4.w & MD_INDEX_MASK]);
             a.gx = a.gy = a.gz = make_float2(0.f, 0.f);
             lj_pack2(pix, piy, piz, pa, pb, nsoff[e4.x >> MD_CODE_SHIFT], nsoff[e4.y >> MD_CODE_SHIFT], e4.x, e4.y,
                      ns2, rc2f, band, a, am);
@@ -997,7 +932,6 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
             fy.add(a.gy.x + a.gy.y);
             fz.add(a.gz.x + a.gz.y);
         }
-#endif
         if (am.n > 0) {  // near-cut-off candidates: FP64 decision in the canonical frame
             const bool listed = am.n <= MD_AMB;
             const int m = listed ? am.n : cnt;
@@ -1024,12 +958,12 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
         npairs = 0.5 * nin;
     }
     warp_partial(partials, pstride, 0, up);
-    warp_partial(partials, pstride, 1, 0.0);
+    warp_partial_zero(partials, pstride, 1);
     warp_partial(partials, pstride, 2, vir);
-    warp_partial(partials, pstride, 3, 0.0);
-    warp_partial(partials, pstride, 4, npairs);
-    warp_partial(partials, pstride, 5, npairs);
-    for (int sl = 6; sl < 12; ++sl) warp_partial(partials, pstride, sl, 0.0);
+    warp_partial_zero(partials, pstride, 3);
+    warp_partial_count(partials, pstride, 4, (float)npairs);
+    warp_partial_count(partials, pstride, 5, (float)npairs);
+    for (int sl = 6; sl < 12; ++sl) warp_partial_zero(partials, pstride, sl);
 }
 
 // FP64 variant: absolute FP64 positions with the reference's halo image
@@ -1078,12 +1012,12 @@ __global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __res
         S.Vx[i] = 0.5 * vx; S.Vy[i] = 0.5 * vy; S.Vz[i] = 0.5 * vz;
     }
     warp_partial(partials, pstride, 0, up);
-    warp_partial(partials, pstride, 1, 0.0);
+    warp_partial_zero(partials, pstride, 1);
     warp_partial(partials, pstride, 2, vir);
-    warp_partial(partials, pstride, 3, 0.0);
-    warp_partial(partials, pstride, 4, (double)nmol);
-    warp_partial(partials, pstride, 5, (double)npairs);
-    for (int sl = 6; sl < 12; ++sl) warp_partial(partials, pstride, sl, 0.0);
+    warp_partial_zero(partials, pstride, 3);
+    warp_partial_count(partials, pstride, 4, (float)nmol);
+    warp_partial_count(partials, pstride, 5, (float)npairs);
+    for (int sl = 6; sl < 12; ++sl) warp_partial_zero(partials, pstride, sl);
 }
 
 // General multi-site molecules: all site pairs of every molecule pair inside
