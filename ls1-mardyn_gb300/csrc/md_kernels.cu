@@ -80,12 +80,62 @@ __device__ __forceinline__ void warp_partial_zero(double* partials, int pstride,
         partials[(size_t)slot * pstride + ((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5)] = 0.0;
 }
 
+// FP64 instructions are scarce on this GPU: a warp-wide FP64 operation
+// holds its sub-partition's FP64 pipe for about 64 cycles (measured: the
+// FP64 pipe of a pair kernel was 53 % busy with 72 FP64 warp instructions
+// per molecule).  The FP32 pair kernels therefore combine and convert their
+// per-molecule and per-warp results with FP32 and integer instructions.
+
+// Exact float -> double conversion on the integer pipes: sign, exponent
+// re-biased by 1023 - 127, mantissa moved up by 52 - 23 bits.  Zero stays
+// (signed) zero, subnormal floats (|x| < 1.18e-38) become zero, infinities
+// and NaNs stay infinities and NaNs.
+__device__ __forceinline__ double f2d_exact(float x) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t ex = (b >> 23) & 0xffu;
+    const uint64_t sign = (uint64_t)(b >> 31) << 63;
+    const uint64_t man = (uint64_t)(b & 0x7fffffu) << 29;
+    const uint64_t e64 = ex == 0xffu ? 0x7ffull : (uint64_t)(ex + 896u);
+    const uint64_t r = ex == 0u ? sign : (sign | (e64 << 52) | man);
+    return __longlong_as_double((long long)r);
+}
+
+// Error-free FP32 sum over the warp of per-lane values hi + lo: a butterfly
+// whose every level adds the hi parts with TwoSum (Knuth) and carries the
+// rounding error into lo.  Every lane ends with the same total hi + lo
+// (TwoSum's error term is exact, so both partners of a level compute it
+// alike), accurate to about 2^-44 relative.
+__device__ __forceinline__ void twosum_xor(float& hi, float& lo, int o) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    const float s = __fadd_rn(hi, h2);
+    const float bp = __fadd_rn(s, -hi);
+    const float err = __fadd_rn(__fadd_rn(hi, -__fadd_rn(s, -bp)), __fadd_rn(h2, -bp));
+    hi = s;
+    lo = __fadd_rn(__fadd_rn(lo, l2), err);
+}
+
+__device__ __forceinline__ void warp_twosum(float& hi, float& lo) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) twosum_xor(hi, lo, o);
+}
+
+// Per-warp partial of an FP32 per-lane value: compensated FP32 warp sum,
+// one FP64 addition (lane 0) to store hi + lo.
+__device__ __forceinline__ void warp_partial_f32(double* partials, int pstride, int slot, float v) {
+    float hi = v, lo = 0.f;
+    warp_twosum(hi, lo);
+    if ((threadIdx.x & 31) == 0)
+        partials[(size_t)slot * pstride + ((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5)] =
+            f2d_exact(hi) + f2d_exact(lo);
+}
+
 // Integer-valued partial (a pair count): reduced exactly in FP32 across the
 // warp (|sum| < 2^24), converted once.
 __device__ __forceinline__ void warp_partial_count(double* partials, int pstride, int slot, float v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0)
-        partials[(size_t)slot * pstride + ((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5)] = (double)v;
+        partials[(size_t)slot * pstride + ((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5)] = f2d_exact(v);
 }
 
 // Sum `v` over the block (blockDim multiple of 32, <= 1024); result valid in thread 0.
@@ -682,8 +732,8 @@ __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __
         const float rclj2 = cP.rclj2f, rc2 = cP.rc2f;
         const float band_lj = cP.band_hi_lj - cP.rclj2f, band_rc = cP.band_hi - cP.rc2f;
         const bool one_comp = cP.ncomp == 1, same_cut = cP.rc2 == cP.rclj2;
-        float e24 = (float)cP.eps24[gi * cP.nlj + gi], s2 = (float)cP.sig2[gi * cP.nlj + gi];
-        float sh6 = (float)cP.shift6[gi * cP.nlj + gi];
+        float e24 = cP.eps24f[gi * cP.nlj + gi], s2 = cP.sig2f[gi * cP.nlj + gi];
+        float sh6 = cP.shift6f[gi * cP.nlj + gi];
         int cur = gi;
         const uint4* row = reinterpret_cast<const uint4*>(nbr + (size_t)i * maxnb);
         for (int k = 0; k < cnt; k += 4) {
@@ -720,9 +770,9 @@ __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __
                     const int gj = cP.comp[__float_as_int(pj[t].w)].ljoff;
                     if (gj != cur) {
                         cur = gj;
-                        e24 = (float)cP.eps24[gi * cP.nlj + gj];
-                        s2 = (float)cP.sig2[gi * cP.nlj + gj];
-                        sh6 = (float)cP.shift6[gi * cP.nlj + gj];
+                        e24 = cP.eps24f[gi * cP.nlj + gj];
+                        s2 = cP.sig2f[gi * cP.nlj + gj];
+                        sh6 = cP.shift6f[gi * cP.nlj + gj];
                     }
                 }
                 // VCP::_loopBodyLJ: scale = eps24 / r^2 (2 lj12 - lj6)
@@ -744,13 +794,13 @@ __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __
             fx.add(gx); fy.add(gy); fz.add(gz);
         }
         if (same_cut) nmol = npairs;
-        S.Fx[i] = fx.value(); S.Fy[i] = fy.value(); S.Fz[i] = fz.value();
+        S.Fx[i] = f2d_exact(fx.s - fx.c); S.Fy[i] = f2d_exact(fy.s - fy.c); S.Fz[i] = f2d_exact(fz.s - fz.c);
         S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
-        S.Vx[i] = 0.5 * (double)vx; S.Vy[i] = 0.5 * (double)vy; S.Vz[i] = 0.5 * (double)vz;
+        S.Vx[i] = f2d_exact(0.5f * vx); S.Vy[i] = f2d_exact(0.5f * vy); S.Vz[i] = f2d_exact(0.5f * vz);
     }
-    warp_partial(partials, pstride, 0, (double)up);
+    warp_partial_f32(partials, pstride, 0, up);
     warp_partial_zero(partials, pstride, 1);
-    warp_partial(partials, pstride, 2, (double)vir);
+    warp_partial_f32(partials, pstride, 2, vir);
     warp_partial_zero(partials, pstride, 3);
     warp_partial_count(partials, pstride, 4, (float)nmol);
     warp_partial_count(partials, pstride, 5, (float)npairs);
@@ -900,12 +950,12 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
     }
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double up = 0.0, vir = 0.0, npairs = 0.0;
+    float up = 0.f, vir = 0.f, npairs = 0.f;  // halved per-molecule sums (every pair is seen twice)
     if (i < S.n) {
         const float4 p4 = xlf[i];
         const int gi = cP.comp[__float_as_int(p4.w)].ljoff;
-        const float e24 = (float)cP.eps24[gi * cP.nlj + gi], s2 = (float)cP.sig2[gi * cP.nlj + gi];
-        const double sh6 = cP.shift6[gi * cP.nlj + gi];
+        const float e24 = cP.eps24f[gi * cP.nlj + gi], s2 = cP.sig2f[gi * cP.nlj + gi];
+        const float sh6 = cP.shift6f[gi * cP.nlj + gi];
         const float2 pix = make_float2(p4.x, p4.x), piy = make_float2(p4.y, p4.y), piz = make_float2(p4.z, p4.z);
         const float2 ns2 = make_float2(-s2, -s2);
         const float rc2f = cP.rclj2f, band = cP.band_hi_lj - cP.rclj2f;
@@ -946,23 +996,24 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
                 if (fp64_r2_canon(S, i, j, code) < cP.rclj2) lj_one(dx, dy, dz, r2, s2, fx, fy, fz, a);
             }
         }
-        const double e = (double)e24;
-        const double nin = (double)(a.nin.x + a.nin.y);
-        const double vx = e * (double)(a.vx.x + a.vx.y), vy = e * (double)(a.vy.x + a.vy.y),
-                     vz = e * (double)(a.vz.x + a.vz.y);
-        S.Fx[i] = e * fx.value(); S.Fy[i] = e * fy.value(); S.Fz[i] = e * fz.value();
+        // epilogue in FP32 (the precision of the pair sums) with exact conversions to the FP64 state
+        const float nin = a.nin.x + a.nin.y;
+        const float vx = e24 * (a.vx.x + a.vx.y), vy = e24 * (a.vy.x + a.vy.y), vz = e24 * (a.vz.x + a.vz.y);
+        S.Fx[i] = f2d_exact(e24 * (fx.s - fx.c));
+        S.Fy[i] = f2d_exact(e24 * (fy.s - fy.c));
+        S.Fz[i] = f2d_exact(e24 * (fz.s - fz.c));
         S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
-        S.Vx[i] = 0.5 * vx; S.Vy[i] = 0.5 * vy; S.Vz[i] = 0.5 * vz;
-        up = 0.5 * (e * (double)(a.up.x + a.up.y) + sh6 * nin);
-        vir = 0.5 * (vx + vy + vz);
-        npairs = 0.5 * nin;
+        S.Vx[i] = f2d_exact(0.5f * vx); S.Vy[i] = f2d_exact(0.5f * vy); S.Vz[i] = f2d_exact(0.5f * vz);
+        up = 0.5f * (e24 * (a.up.x + a.up.y) + sh6 * nin);
+        vir = 0.5f * (vx + (vy + vz));
+        npairs = 0.5f * nin;
     }
-    warp_partial(partials, pstride, 0, up);
+    warp_partial_f32(partials, pstride, 0, up);
     warp_partial_zero(partials, pstride, 1);
-    warp_partial(partials, pstride, 2, vir);
+    warp_partial_f32(partials, pstride, 2, vir);
     warp_partial_zero(partials, pstride, 3);
-    warp_partial_count(partials, pstride, 4, (float)npairs);
-    warp_partial_count(partials, pstride, 5, (float)npairs);
+    warp_partial_count(partials, pstride, 4, npairs);
+    warp_partial_count(partials, pstride, 5, npairs);
     for (int sl = 6; sl < 12; ++sl) warp_partial_zero(partials, pstride, sl);
 }
 
@@ -1020,15 +1071,181 @@ __global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __res
     for (int sl = 6; sl < 12; ++sl) warp_partial_zero(partials, pstride, sl);
 }
 
+// ---------------------------------------------------------------- multi-site
+// Multi-site molecules are processed one warp per molecule: the warp's lanes
+// share the molecule's component (its site loops are warp-uniform), and the
+// candidate rows are stably partitioned by the neighbour's component after
+// every list build, so consecutive candidates also share the neighbour's site
+// loops.  The candidates inside a cut-off are compacted into a per-warp ring
+// in row order before the site-pair work, so no lane idles on a candidate
+// beyond the cut-off.
+
+// Stable partition of every candidate row by the neighbour's component (one
+// warp per molecule; the row is staged in dynamic shared memory, maxnb
+// entries per warp).  Only the order within a row changes.
+__global__ void k_row_partition(int64_t n, const float4* __restrict__ xl, uint32_t* nbr, const int* nnb, int maxnb,
+                                int ncomp, const unsigned* need) {
+    if (!*need) return;
+    extern __shared__ uint32_t rowbuf[];
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + wl;
+    if (i >= n) return;  // warp-uniform
+    uint32_t* buf = rowbuf + (size_t)wl * maxnb;
+    uint32_t* row = nbr + (size_t)i * maxnb;
+    const int cnt = nnb[i];
+    for (int k = lane; k < cnt; k += 32) buf[k] = row[k];
+    __syncwarp();
+    int out = 0;
+    for (int c = 0; c < ncomp; ++c) {
+        for (int k0 = 0; k0 < cnt; k0 += 32) {
+            const int k = k0 + lane;
+            uint32_t e = 0u;
+            bool m = false;
+            if (k < cnt) {
+                e = buf[k];
+                m = __float_as_int(__ldg(&xl[e & MD_INDEX_MASK]).w) == c;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, m);
+            if (m) row[out + __popc(bal & ((1u << lane) - 1u))] = e;
+            out += __popc(bal);
+        }
+    }
+}
+
+// Centre distance m_d = r_i - (r_j + image) of candidate e: FP32 local
+// coordinates with the cell offset (mixed precision) or FP64 positions with
+// the reference's halo shift.
+template <typename Real>
+__device__ __forceinline__ void ms_centre_distance(const State& S, const float4* xlf, const Real (*soff)[3],
+                                                   const Real* pi, int64_t i, uint32_t e, Real* md) {
+    const int64_t j = e & MD_INDEX_MASK;
+    const uint32_t code = e >> MD_CODE_SHIFT;
+    if (sizeof(Real) == 4) {
+        const float4 pj = __ldg(&xlf[j]);
+        md[0] = (pi[0] - (Real)pj.x) - soff[code][0];
+        md[1] = (pi[1] - (Real)pj.y) - soff[code][1];
+        md[2] = (pi[2] - (Real)pj.z) - soff[code][2];
+    } else {
+        double shf[3];
+        image_shift(S.home[i], code, shf);
+        md[0] = pi[0] - (S.rx[j] + shf[0]);
+        md[1] = pi[1] - (S.ry[j] + shf[1]);
+        md[2] = pi[2] - (S.rz[j] + shf[2]);
+    }
+}
+
+// Cut-off flags of a candidate (bit 0: inside rc_lj, bit 1: inside rc); in
+// mixed precision FP32 r^2 near a cut-off is re-decided in FP64 in the
+// pair's canonical frame.
+template <typename Real>
+__device__ __forceinline__ int ms_flags(const State& S, int64_t i, uint32_t e, const Real* md) {
+    const Real r2 = md[0] * md[0] + (md[1] * md[1] + md[2] * md[2]);
+    const Real rclj2 = sizeof(Real) == 4 ? (Real)cP.rclj2f : (Real)cP.rclj2;
+    const Real rc2 = sizeof(Real) == 4 ? (Real)cP.rc2f : (Real)cP.rc2;
+    bool lj_on = r2 < rclj2, el_on = r2 < rc2;
+    if (sizeof(Real) == 4) {
+        const bool bl = r2 > (Real)cP.band_lo_lj && r2 < (Real)cP.band_hi_lj;
+        const bool be = r2 > (Real)cP.band_lo && r2 < (Real)cP.band_hi;
+        if (bl || be) {
+            const double r2d = fp64_r2_canon(S, i, e & MD_INDEX_MASK, e >> MD_CODE_SHIFT);
+            if (bl) lj_on = r2d < cP.rclj2;
+            if (be) el_on = r2d < cP.rc2;
+        }
+    }
+    return (lj_on ? 1 : 0) | (el_on ? 2 : 0);
+}
+
+// Walk molecule i's candidate row with the whole warp: each lane tests one
+// candidate per round; candidates inside a cut-off enter the warp's ring of
+// 64 (entry + flags) in row order; every full group of 32 is handed to
+// `body(entry, flags, m_d)`, one candidate per lane, and the rest (< 32) at
+// the end to the lanes below the count.
+template <typename Real, typename Body>
+__device__ __forceinline__ void ms_walk_row(const State& S, const float4* xlf, const Real (*soff)[3], const Real* pi,
+                                            int64_t i, const uint32_t* row, int cnt, uint32_t* ring, int lane,
+                                            Body body) {
+    int head = 0, qn = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int k0 = 0; k0 < cnt; k0 += 32) {
+        const int k = k0 + lane;
+        int fl = 0;
+        uint32_t e = 0u;
+        if (k < cnt) {
+            e = __ldg(&row[k]);
+            Real md[3];
+            ms_centre_distance<Real>(S, xlf, soff, pi, i, e, md);
+            fl = ms_flags<Real>(S, i, e, md);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, fl != 0);
+        if (fl) {
+            const int p = (head + qn + __popc(bal & lt)) & 63;
+            ring[p] = e;
+            ring[64 + p] = (uint32_t)fl;
+        }
+        qn += __popc(bal);
+        __syncwarp();
+        if (qn >= 32) {
+            const int p = (head + lane) & 63;
+            const uint32_t ee = ring[p];
+            const int ff = (int)ring[64 + p];
+            __syncwarp();
+            head = (head + 32) & 63;
+            qn -= 32;
+            Real md[3];
+            ms_centre_distance<Real>(S, xlf, soff, pi, i, ee, md);
+            body(ee, ff, md);
+        }
+    }
+    if (qn > 0) {
+        const int p = (head + lane) & 63;
+        const uint32_t ee = ring[p];
+        const int ff = (int)ring[64 + p];
+        __syncwarp();
+        if (lane < qn) {
+            Real md[3];
+            ms_centre_distance<Real>(S, xlf, soff, pi, i, ee, md);
+            body(ee, ff, md);
+        }
+    }
+    __syncwarp();
+}
+
+// Total over the warp of a per-lane compensated FP32 sum (rounded to FP32,
+// the precision of the pair arithmetic) or plain FP64 sum; valid in lane 0.
+// `scale` is a power of two (exact).
+__device__ __forceinline__ double warp_total(const KSum& k, float scale = 1.f) {
+    float hi = scale * k.s, lo = -scale * k.c;
+    warp_twosum(hi, lo);
+    return f2d_exact(__fadd_rn(hi, lo));
+}
+__device__ __forceinline__ double warp_total(const DSum& k, float scale = 1.f) { return (double)scale * warp_sum(k.s); }
+
+// Per-warp partial of a per-lane accumulator, times sign (+-1).
+__device__ __forceinline__ void warp_partial_acc(double* partials, int pstride, int slot, const KSum& k, float sign) {
+    float hi = sign * k.s, lo = -sign * k.c;
+    warp_twosum(hi, lo);
+    if ((threadIdx.x & 31) == 0)
+        partials[(size_t)slot * pstride + ((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5)] =
+            f2d_exact(hi) + f2d_exact(lo);
+}
+__device__ __forceinline__ void warp_partial_acc(double* partials, int pstride, int slot, const DSum& k, float sign) {
+    warp_partial(partials, pstride, slot, (double)sign * k.s);
+}
+
+#define MS_WARPS 4     // warps per block of the multi-site kernels
+#define MS_MOLS 32     // molecules per warp, one after another
+
 // General multi-site molecules: all site pairs of every molecule pair inside
 // the molecule-centre cut-off (rc_lj for LJ centres, rc for the multipoles),
 // with calcFM folded in: F = sum f, M = sum d_site x f + multipole torques,
-// Vi = 1/2 sum m_d o f.
+// Vi = 1/2 sum m_d o f.  Per lane the sums are compensated (FP32) or plain
+// (FP64); per molecule the 32 lanes are combined in FP64 in a fixed order.
 template <typename Real>
-__global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, const Real* sd, const Real* se,
-                                                  int stride, const uint32_t* nbr, const int* nnb, int maxnb,
-                                                  double* partials, int pstride) {
+__global__ void __launch_bounds__(MS_WARPS * 32) k_force_ms(State S, const float4* xlf, const Real* sd, const Real* se,
+                                                            int stride, const uint32_t* nbr, const int* nnb, int maxnb,
+                                                            double* partials, int pstride) {
     __shared__ Real soff[27][3];
+    __shared__ uint32_t ring[MS_WARPS][128];
     if (threadIdx.x < 27) {
         int t = threadIdx.x;
         soff[t][0] = (Real)((t % 3 - 1) * cP.lside[0]);
@@ -1036,54 +1253,29 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
         soff[t][2] = (Real)((t / 9 - 1) * cP.lside[2]);
     }
     __syncthreads();
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    typename Acc<Real>::type F[3], M[3], V[3], u6, ux, vir, rf;
-    for (int e = 0; e < 3; ++e) { F[e].init(); M[e].init(); V[e].init(); }
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t w = (int64_t)blockIdx.x * MS_WARPS + wl;
+    typename Acc<Real>::type u6, ux, vir, rf;
     u6.init(); ux.init(); vir.init(); rf.init();
     int cnt_pairs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (i < S.n) {
+    const Real epsRF = (Real)cP.epsRFInvrc3;
+    for (int t = 0; t < MS_MOLS; ++t) {
+        const int64_t i = w * MS_MOLS + t;
+        if (i >= S.n) break;  // warp-uniform
         const int ci = S.comp[i];
         const CompDev& A = cP.comp[ci];
         Real pi[3];
         if (sizeof(Real) == 4) {
-            float4 p = xlf[i];
+            const float4 p = xlf[i];
             pi[0] = p.x; pi[1] = p.y; pi[2] = p.z;
         } else {
             pi[0] = S.rx[i]; pi[1] = S.ry[i]; pi[2] = S.rz[i];
         }
-        const int cnt = nnb[i];
-        const Real rclj2 = sizeof(Real) == 4 ? (Real)cP.rclj2f : (Real)cP.rclj2;
-        const Real rc2 = sizeof(Real) == 4 ? (Real)cP.rc2f : (Real)cP.rc2;
-        const Real epsRF = (Real)cP.epsRFInvrc3;
-        for (int k = 0; k < cnt; ++k) {
-            uint32_t e = __ldg(&nbr[(size_t)i * maxnb + k]);
-            int64_t j = e & MD_INDEX_MASK;
-            uint32_t code = e >> MD_CODE_SHIFT;
-            Real md[3];
-            if (sizeof(Real) == 4) {
-                float4 pj = __ldg(&xlf[j]);
-                md[0] = (pi[0] - (Real)pj.x) - soff[code][0];
-                md[1] = (pi[1] - (Real)pj.y) - soff[code][1];
-                md[2] = (pi[2] - (Real)pj.z) - soff[code][2];
-            } else {
-                double shf[3];
-                image_shift(S.home[i], code, shf);
-                md[0] = pi[0] - (S.rx[j] + shf[0]);
-                md[1] = pi[1] - (S.ry[j] + shf[1]);
-                md[2] = pi[2] - (S.rz[j] + shf[2]);
-            }
-            Real r2 = md[0] * md[0] + (md[1] * md[1] + md[2] * md[2]);
-            bool lj_on = r2 < rclj2, el_on = r2 < rc2;
-            if (sizeof(Real) == 4) {
-                bool bl = r2 > (Real)cP.band_lo_lj && r2 < (Real)cP.band_hi_lj;
-                bool be = r2 > (Real)cP.band_lo && r2 < (Real)cP.band_hi;
-                if (bl || be) {
-                    double r2d = fp64_r2(S, i, j, code);
-                    if (bl) lj_on = r2d < cP.rclj2;
-                    if (be) el_on = r2d < cP.rc2;
-                }
-            }
-            if (!lj_on && !el_on) continue;
+        typename Acc<Real>::type F[3], M[3], V[3];
+        for (int c = 0; c < 3; ++c) { F[c].init(); M[c].init(); V[c].init(); }
+        auto body = [&](uint32_t e, int fl, const Real* md) {
+            const int64_t j = e & MD_INDEX_MASK;
+            const bool lj_on = fl & 1, el_on = (fl & 2) != 0;
             const int cj = S.comp[j];
             const CompDev& B = cP.comp[cj];
             const bool macro = j > i;
@@ -1108,8 +1300,8 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
                     Real f[3], Vp[3], T[3] = {0, 0, 0}, u = 0, urf = 0;
                     int kind;
                     if (ka == SK_LJ) {
-                        int ga = A.ljoff + a, gb = B.ljoff + b;
-                        Real s2r = dsite[0] * dsite[0] + (dsite[1] * dsite[1] + dsite[2] * dsite[2]);
+                        const int ga = A.ljoff + a, gb = B.ljoff + b;
+                        const Real s2r = dsite[0] * dsite[0] + (dsite[1] * dsite[1] + dsite[2] * dsite[2]);
                         lj_pair<Real>(dsite, md, s2r, PTab<Real>::eps24(cP, ga * cP.nlj + gb),
                                       PTab<Real>::sig2(cP, ga * cP.nlj + gb), PTab<Real>::shift6(cP, ga * cP.nlj + gb), f,
                                       Vp, u);
@@ -1128,34 +1320,59 @@ __global__ void __launch_bounds__(128) k_force_ms(State S, const float4* xlf, co
                     }
                 }
                 // torque of the site forces about the centre plus the multipole torque
-                Real cx = da[1] * fa[2] - da[2] * fa[1];
-                Real cy = da[2] * fa[0] - da[0] * fa[2];
-                Real cz = da[0] * fa[1] - da[1] * fa[0];
+                const Real cx = da[1] * fa[2] - da[2] * fa[1];
+                const Real cy = da[2] * fa[0] - da[0] * fa[2];
+                const Real cz = da[0] * fa[1] - da[1] * fa[0];
                 M[0].add(cx + ta[0]); M[1].add(cy + ta[1]); M[2].add(cz + ta[2]);
             }
+        };
+        ms_walk_row<Real>(S, xlf, soff, pi, i, nbr + (size_t)i * maxnb, nnb[i], ring[wl], lane, body);
+        const double fx = warp_total(F[0]), fy = warp_total(F[1]), fz = warp_total(F[2]);
+        const double mx = warp_total(M[0]), my = warp_total(M[1]), mz = warp_total(M[2]);
+        const double vx = warp_total(V[0], 0.5f), vy = warp_total(V[1], 0.5f), vz = warp_total(V[2], 0.5f);
+        if (lane == 0) {
+            S.Fx[i] = fx; S.Fy[i] = fy; S.Fz[i] = fz;
+            S.Mx[i] = mx; S.My[i] = my; S.Mz[i] = mz;
+            S.Vx[i] = vx; S.Vy[i] = vy; S.Vz[i] = vz;
         }
-        S.Fx[i] = F[0].value(); S.Fy[i] = F[1].value(); S.Fz[i] = F[2].value();
-        S.Mx[i] = M[0].value(); S.My[i] = M[1].value(); S.Mz[i] = M[2].value();
-        S.Vx[i] = 0.5 * V[0].value(); S.Vy[i] = 0.5 * V[1].value(); S.Vz[i] = 0.5 * V[2].value();
     }
-    warp_partial(partials, pstride, 0, u6.value());
-    warp_partial(partials, pstride, 1, ux.value());
-    warp_partial(partials, pstride, 2, vir.value());
-    warp_partial(partials, pstride, 3, -rf.value());
-    for (int sl = 0; sl < 8; ++sl) warp_partial(partials, pstride, 4 + sl, (double)cnt_pairs[sl]);
+    warp_partial_acc(partials, pstride, 0, u6, 1.f);
+    warp_partial_acc(partials, pstride, 1, ux, 1.f);
+    warp_partial_acc(partials, pstride, 2, vir, 1.f);
+    warp_partial_acc(partials, pstride, 3, rf, -1.f);
+    for (int sl = 0; sl < 8; ++sl) warp_partial_count(partials, pstride, 4 + sl, (float)cnt_pairs[sl]);
 }
 
 // ------------------------------------------------------------------ integration
+// Time-step constants of the half steps, computed on the host: dt/2 and
+// dt/(2m) per component, the latter with the same IEEE division the
+// reference performs per molecule (a device FP64 division costs about ten
+// FP64 instructions per molecule, and FP64 throughput bounds these kernels).
+struct Kick {
+    double dt, dt_halve;
+    double dtInv2m[MD_MAXC];
+};
+
+// dt/(2m) of component c by selects over the parameter (a dynamic index
+// into a kernel parameter would copy it to local memory)
+__device__ __forceinline__ double kick_dtInv2m(const Kick& K, int c) {
+    double r = K.dtInv2m[0];
+#pragma unroll
+    for (int k = 1; k < MD_MAXC; ++k) r = c == k ? K.dtInv2m[k] : r;
+    return r;
+}
+
 // FullMolecule::upd_preF; afterwards the FP32 local coordinates and the
 // displacement since the last list build (for the rebuild test).
-__global__ void k_pre(State S, double dt, float4* xlf, const double* origin, const float4* xlref, unsigned* disp_max) {
+__global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const float4* xlref, unsigned* disp_max) {
     __shared__ float smax[8];
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float d2 = 0.f;
     if (i < S.n) {
-        const CompDev& C = cP.comp[S.comp[i]];
-        double dt_halve = .5 * dt;
-        double dtInv2m = dt_halve / C.m;
+        const int ci = S.comp[i];
+        const CompDev& C = cP.comp[ci];
+        const double dt = K.dt, dt_halve = K.dt_halve;
+        const double dtInv2m = kick_dtInv2m(K, ci);
         double vx = S.vx[i] + dtInv2m * S.Fx[i];
         double vy = S.vy[i] + dtInv2m * S.Fy[i];
         double vz = S.vz[i] + dtInv2m * S.Fz[i];
@@ -1230,13 +1447,14 @@ __global__ void k_sum_int(const int* a, int64_t n, unsigned long long* out) {
 }
 
 // FullMolecule::upd_postF with the Leapfrog sums.
-__global__ void k_post(State S, double dt, double* partials, int pstride) {
+__global__ void k_post(State S, Kick K, double* partials, int pstride) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double mv2 = 0.0, iw2 = 0.0;
     if (i < S.n) {
-        const CompDev& C = cP.comp[S.comp[i]];
-        double dt_halve = 0.5 * dt;
-        double dtInv2m = dt_halve / C.m;
+        const int ci = S.comp[i];
+        const CompDev& C = cP.comp[ci];
+        const double dt_halve = K.dt_halve;
+        const double dtInv2m = kick_dtInv2m(K, ci);
         double v[3] = {S.vx[i], S.vy[i], S.vz[i]};
         double F[3] = {S.Fx[i], S.Fy[i], S.Fz[i]};
         double v2 = 0.;
@@ -1265,16 +1483,17 @@ __global__ void k_post(State S, double dt, double* partials, int pstride) {
 // molecule rotates (both half kicks use the same F): the same FP64
 // operations in the same order as k_post followed by k_pre, one pass over
 // the state instead of two.
-__global__ void k_post_pre(State S, double dt, double* partials, int pstride, float4* xlf, const double* origin,
+__global__ void k_post_pre(State S, Kick K, double* partials, int pstride, float4* xlf, const double* origin,
                            const float4* xlref, unsigned* disp_max) {
     __shared__ float smax[8];
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double mv2 = 0.0;
     float d2 = 0.f;
     if (i < S.n) {
-        const CompDev& C = cP.comp[S.comp[i]];
-        const double dt_halve = 0.5 * dt;
-        const double dtInv2m = dt_halve / C.m;
+        const int ci = S.comp[i];
+        const CompDev& C = cP.comp[ci];
+        const double dt = K.dt;
+        const double dtInv2m = kick_dtInv2m(K, ci);
         const double F[3] = {S.Fx[i], S.Fy[i], S.Fz[i]};
         double v[3] = {S.vx[i], S.vy[i], S.vz[i]};
         double v2 = 0.;
