@@ -887,16 +887,16 @@ __device__ __forceinline__ float r2_scalar(const float4 pi, const float4 pj, flo
 }
 
 __device__ __forceinline__ void lj_pack2(const float2 pix, const float2 piy, const float2 piz,
-                                         const float4 pa, const float4 pb, const float4 oa, const float4 ob,
-                                         uint32_t ea, uint32_t eb, const float2 ns2, const float rc2f,
+                                         const float4 pa, const float4 pb, const float2 ox, const float2 oy,
+                                         const float2 oz, uint32_t ea, uint32_t eb, const float2 ns2, const float rc2f,
                                          const float band, LjPack& a, AmbList& am) {
     const float2 m1 = make_float2(-1.f, -1.f);
     float2 dx = __ffma2_rn(make_float2(pa.x, pb.x), m1, pix);
     float2 dy = __ffma2_rn(make_float2(pa.y, pb.y), m1, piy);
     float2 dz = __ffma2_rn(make_float2(pa.z, pb.z), m1, piz);
-    dx = __fadd2_rn(dx, make_float2(oa.x, ob.x));
-    dy = __fadd2_rn(dy, make_float2(oa.y, ob.y));
-    dz = __fadd2_rn(dz, make_float2(oa.z, ob.z));
+    dx = __fadd2_rn(dx, ox);
+    dy = __fadd2_rn(dy, oy);
+    dz = __fadd2_rn(dz, oz);
     float2 r2 = __fmul2_rn(dz, dz);
     r2 = __ffma2_rn(dy, dy, r2);
     r2 = __ffma2_rn(dx, dx, r2);
@@ -942,11 +942,15 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
                                                          const uint32_t* __restrict__ nbr,
                                                          const int* __restrict__ nnb, int maxnb, double* partials,
                                                          int pstride) {
-    __shared__ float4 nsoff[27];  // minus the offset of neighbour cell origin (code) from the home cell origin
-    if (threadIdx.x < 27) {
-        int t = threadIdx.x;
-        nsoff[t] = make_float4((float)(-(t % 3 - 1) * cP.lside[0]), (float)(-((t / 3) % 3 - 1) * cP.lside[1]),
-                               (float)(-(t / 9 - 1) * cP.lside[2]), 0.f);
+    // minus the offset of the neighbour cell's origin (code) from the home cell's origin, one table per
+    // axis: three conflict-free 4-byte shared loads per candidate move fewer shared-memory wavefronts
+    // than one 16-byte load (which also conflicts between codes 8 apart)
+    __shared__ float nsx[32], nsy[32], nsz[32];
+    if (threadIdx.x < 32) {
+        const int t = threadIdx.x < 27 ? threadIdx.x : 13;
+        nsx[threadIdx.x] = (float)(-(t % 3 - 1) * cP.lside[0]);
+        nsy[threadIdx.x] = (float)(-((t / 3) % 3 - 1) * cP.lside[1]);
+        nsz[threadIdx.x] = (float)(-(t / 9 - 1) * cP.lside[2]);
     }
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -974,10 +978,12 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
             const float4 pa = __ldg(&xlf[e4.x & MD_INDEX_MASK]), pb = __ldg(&xlf[e4.y & MD_INDEX_MASK]);
             const float4 pc = __ldg(&xlf[e4.z & MD_INDEX_MASK]), pd = __ldg(&xlf[e4.w & MD_INDEX_MASK]);
             a.gx = a.gy = a.gz = make_float2(0.f, 0.f);
-            lj_pack2(pix, piy, piz, pa, pb, nsoff[e4.x >> MD_CODE_SHIFT], nsoff[e4.y >> MD_CODE_SHIFT], e4.x, e4.y,
-                     ns2, rc2f, band, a, am);
-            lj_pack2(pix, piy, piz, pc, pd, nsoff[e4.z >> MD_CODE_SHIFT], nsoff[e4.w >> MD_CODE_SHIFT], e4.z, e4.w,
-                     ns2, rc2f, band, a, am);
+            const uint32_t ca = e4.x >> MD_CODE_SHIFT, cb = e4.y >> MD_CODE_SHIFT;
+            const uint32_t cc = e4.z >> MD_CODE_SHIFT, cd = e4.w >> MD_CODE_SHIFT;
+            lj_pack2(pix, piy, piz, pa, pb, make_float2(nsx[ca], nsx[cb]), make_float2(nsy[ca], nsy[cb]),
+                     make_float2(nsz[ca], nsz[cb]), e4.x, e4.y, ns2, rc2f, band, a, am);
+            lj_pack2(pix, piy, piz, pc, pd, make_float2(nsx[cc], nsx[cd]), make_float2(nsy[cc], nsy[cd]),
+                     make_float2(nsz[cc], nsz[cd]), e4.z, e4.w, ns2, rc2f, band, a, am);
             fx.add(a.gx.x + a.gx.y);
             fy.add(a.gy.x + a.gy.y);
             fz.add(a.gz.x + a.gz.y);
@@ -989,9 +995,8 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
                 const uint32_t en = listed ? am.e[t] : nbr[(size_t)i * maxnb + t];
                 const int j = (int)(en & MD_INDEX_MASK);
                 const uint32_t code = en >> MD_CODE_SHIFT;
-                const float4 o = nsoff[code];
                 float dx, dy, dz;
-                const float r2 = r2_scalar(p4, __ldg(&xlf[j]), o.x, o.y, o.z, dx, dy, dz);
+                const float r2 = r2_scalar(p4, __ldg(&xlf[j]), nsx[code], nsy[code], nsz[code], dx, dy, dz);
                 if (!(fabsf(r2 - rc2f) < band)) continue;  // (row scan) not near the cut-off
                 if (fp64_r2_canon(S, i, j, code) < cP.rclj2) lj_one(dx, dy, dz, r2, s2, fx, fy, fz, a);
             }
@@ -1246,6 +1251,7 @@ __global__ void __launch_bounds__(MS_WARPS * 32) k_force_ms(State S, const float
                                                             double* partials, int pstride) {
     __shared__ Real soff[27][3];
     __shared__ uint32_t ring[MS_WARPS][128];
+    __shared__ Real site_i[MS_WARPS][2][MD_MAXS][3];  // the warp's molecule: site offsets, orientations
     if (threadIdx.x < 27) {
         int t = threadIdx.x;
         soff[t][0] = (Real)((t % 3 - 1) * cP.lside[0]);
@@ -1259,6 +1265,7 @@ __global__ void __launch_bounds__(MS_WARPS * 32) k_force_ms(State S, const float
     u6.init(); ux.init(); vir.init(); rf.init();
     int cnt_pairs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const Real epsRF = (Real)cP.epsRFInvrc3;
+    const uint32_t sstride = 3u * (uint32_t)stride;  // site arrays are [slot][site][3]; the host keeps cap * stride * 3 < 2^32
     for (int t = 0; t < MS_MOLS; ++t) {
         const int64_t i = w * MS_MOLS + t;
         if (i >= S.n) break;  // warp-uniform
@@ -1271,31 +1278,38 @@ __global__ void __launch_bounds__(MS_WARPS * 32) k_force_ms(State S, const float
         } else {
             pi[0] = S.rx[i]; pi[1] = S.ry[i]; pi[2] = S.rz[i];
         }
+        __syncwarp();
+        if (lane < 3 * A.ns) {
+            site_i[wl][0][lane / 3][lane % 3] = sd[(uint32_t)i * sstride + lane];
+            site_i[wl][1][lane / 3][lane % 3] = se[(uint32_t)i * sstride + lane];
+        }
+        __syncwarp();
         typename Acc<Real>::type F[3], M[3], V[3];
         for (int c = 0; c < 3; ++c) { F[c].init(); M[c].init(); V[c].init(); }
         auto body = [&](uint32_t e, int fl, const Real* md) {
-            const int64_t j = e & MD_INDEX_MASK;
+            const uint32_t j = e & MD_INDEX_MASK;
             const bool lj_on = fl & 1, el_on = (fl & 2) != 0;
             const int cj = S.comp[j];
             const CompDev& B = cP.comp[cj];
-            const bool macro = j > i;
-            if (el_on && macro) cnt_pairs[0] += 1;
+            const bool macro = (int64_t)j > i;
+            // this molecule pair's contributions, added to the compensated sums once
+            Real fp[3] = {0, 0, 0}, mp[3] = {0, 0, 0}, vp[3] = {0, 0, 0};
+            Real u6p = 0, uxp = 0, rfp = 0;
             for (int a = 0; a < A.ns; ++a) {
                 const int ka = A.kind[a];
                 if (ka == SK_LJ && !lj_on) continue;
                 if (ka != SK_LJ && !el_on) continue;
-                Real da[3], ea[3] = {0, 0, 0};
-                for (int c = 0; c < 3; ++c) da[c] = sd[((int64_t)i * stride + a) * 3 + c];
-                if (ka >= SK_DIPOLE)
-                    for (int c = 0; c < 3; ++c) ea[c] = se[((int64_t)i * stride + a) * 3 + c];
+                const Real* da = site_i[wl][0][a];
+                const Real* ea = site_i[wl][1][a];
                 Real fa[3] = {0, 0, 0}, ta[3] = {0, 0, 0};
                 for (int b = 0; b < B.ns; ++b) {
                     const int kb = B.kind[b];
                     if ((ka == SK_LJ) != (kb == SK_LJ)) continue;
+                    const uint32_t ob = j * sstride + 3u * (uint32_t)b;
                     Real db[3], eb[3] = {0, 0, 0};
-                    for (int c = 0; c < 3; ++c) db[c] = sd[((int64_t)j * stride + b) * 3 + c];
+                    for (int c = 0; c < 3; ++c) db[c] = sd[ob + c];
                     if (kb >= SK_DIPOLE)
-                        for (int c = 0; c < 3; ++c) eb[c] = se[((int64_t)j * stride + b) * 3 + c];
+                        for (int c = 0; c < 3; ++c) eb[c] = se[ob + c];
                     Real dsite[3] = {md[0] + (da[0] - db[0]), md[1] + (da[1] - db[1]), md[2] + (da[2] - db[2])};
                     Real f[3], Vp[3], T[3] = {0, 0, 0}, u = 0, urf = 0;
                     int kind;
@@ -1305,25 +1319,30 @@ __global__ void __launch_bounds__(MS_WARPS * 32) k_force_ms(State S, const float
                         lj_pair<Real>(dsite, md, s2r, PTab<Real>::eps24(cP, ga * cP.nlj + gb),
                                       PTab<Real>::sig2(cP, ga * cP.nlj + gb), PTab<Real>::shift6(cP, ga * cP.nlj + gb), f,
                                       Vp, u);
-                        if (macro) u6.add(u);
+                        u6p += u;
                         kind = 0;
                     } else {
                         kind = multipole_pair<Real>(ka, kb, dsite, md, PTab<Real>::p(cP, ci, a), ea,
                                                     PTab<Real>::p(cP, cj, b), eb, epsRF, f, Vp, T, u, urf);
-                        if (macro) { ux.add(u); rf.add(urf); }
+                        uxp += u;
+                        rfp += urf;
                     }
-                    for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
-                    for (int c = 0; c < 3; ++c) { F[c].add(f[c]); V[c].add(Vp[c]); }
-                    if (macro) {
-                        vir.add(Vp[0] + Vp[1] + Vp[2]);
-                        cnt_pairs[1 + kind] += 1;
-                    }
+                    for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; vp[c] += Vp[c]; }
+                    if (macro) cnt_pairs[1 + kind] += 1;
                 }
                 // torque of the site forces about the centre plus the multipole torque
-                const Real cx = da[1] * fa[2] - da[2] * fa[1];
-                const Real cy = da[2] * fa[0] - da[0] * fa[2];
-                const Real cz = da[0] * fa[1] - da[1] * fa[0];
-                M[0].add(cx + ta[0]); M[1].add(cy + ta[1]); M[2].add(cz + ta[2]);
+                mp[0] += (da[1] * fa[2] - da[2] * fa[1]) + ta[0];
+                mp[1] += (da[2] * fa[0] - da[0] * fa[2]) + ta[1];
+                mp[2] += (da[0] * fa[1] - da[1] * fa[0]) + ta[2];
+                for (int c = 0; c < 3; ++c) fp[c] += fa[c];
+            }
+            for (int c = 0; c < 3; ++c) { F[c].add(fp[c]); M[c].add(mp[c]); V[c].add(vp[c]); }
+            if (macro) {
+                if (el_on) cnt_pairs[0] += 1;
+                u6.add(u6p);
+                ux.add(uxp);
+                rf.add(rfp);
+                vir.add(vp[0] + vp[1] + vp[2]);
             }
         };
         ms_walk_row<Real>(S, xlf, soff, pi, i, nbr + (size_t)i * maxnb, nnb[i], ring[wl], lane, body);

@@ -13,11 +13,23 @@
 
 namespace md {
 
+// FP32: the hardware approximations (about 1 ulp), which the FP32 pair
+// arithmetic tolerates; FP64: IEEE division and square root.
+__device__ __forceinline__ float rcp_approx_f(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrt_approx_f(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 template <typename Real> __device__ __forceinline__ Real rcp_(Real x);
-template <> __device__ __forceinline__ float rcp_<float>(float x) { return __frcp_rn(x); }
+template <> __device__ __forceinline__ float rcp_<float>(float x) { return rcp_approx_f(x); }
 template <> __device__ __forceinline__ double rcp_<double>(double x) { return 1.0 / x; }
 template <typename Real> __device__ __forceinline__ Real sqrt_(Real x);
-template <> __device__ __forceinline__ float sqrt_<float>(float x) { return sqrtf(x); }
+template <> __device__ __forceinline__ float sqrt_<float>(float x) { return sqrt_approx_f(x); }
 template <> __device__ __forceinline__ double sqrt_<double>(double x) { return sqrt(x); }
 
 template <typename Real>
