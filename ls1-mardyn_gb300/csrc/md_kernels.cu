@@ -100,6 +100,25 @@ __device__ __forceinline__ double f2d_exact(float x) {
     return __longlong_as_double((long long)r);
 }
 
+// double -> float conversion, rounded to nearest even, on the integer pipes:
+// the magnitude is rounded at the 29th bit (carries may reach the exponent),
+// the exponent re-biased by 127 - 1023.  Results below FP32's normal range
+// become (signed) zero, results above it infinity; NaN stays NaN.  Equal to
+// the IEEE conversion for every input whose FP32 result is normal, zero,
+// infinite or NaN.
+__device__ __forceinline__ float d2f_int(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long mag = b & 0x7fffffffffffffffull;
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const unsigned long long m = mag + 0x0fffffffull + ((mag >> 29) & 1ull);
+    const int e = (int)(m >> 52) - 896;
+    uint32_t r = sign | ((uint32_t)e << 23) | ((uint32_t)(m >> 29) & 0x7fffffu);
+    r = e >= 255 ? (sign | 0x7f800000u) : r;
+    r = e <= 0 ? sign : r;
+    r = mag > 0x7ff0000000000000ull ? 0x7fc00000u : r;
+    return __uint_as_float(r);
+}
+
 // Error-free FP32 sum over the warp of per-lane values hi + lo: a butterfly
 // whose every level adds the hi parts with TwoSum (Knuth) and carries the
 // rounding error into lo.  Every lane ends with the same total hi + lo
@@ -498,9 +517,9 @@ __global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, con
     double ox = cP.bmin[0] + cx * cP.lside[0], oy = cP.bmin[1] + cy * cP.lside[1], oz = cP.bmin[2] + cz * cP.lside[2];
     origin[3 * i] = ox; origin[3 * i + 1] = oy; origin[3 * i + 2] = oz;
     float4 p;
-    p.x = (float)(S.rx[i] - ox);
-    p.y = (float)(S.ry[i] - oy);
-    p.z = (float)(S.rz[i] - oz);
+    p.x = d2f_int(S.rx[i] - ox);
+    p.y = d2f_int(S.ry[i] - oy);
+    p.z = d2f_int(S.rz[i] - oz);
     p.w = __int_as_float(S.comp[i]);
     xlf[i] = p;
     xlref[i] = p;
@@ -1370,6 +1389,7 @@ __global__ void __launch_bounds__(MS_WARPS * 32) k_force_ms(State S, const float
 struct Kick {
     double dt, dt_halve;
     double dtInv2m[MD_MAXC];
+    float massf[MD_MAXC];
 };
 
 // dt/(2m) of component c by selects over the parameter (a dynamic index
@@ -1378,6 +1398,12 @@ __device__ __forceinline__ double kick_dtInv2m(const Kick& K, int c) {
     double r = K.dtInv2m[0];
 #pragma unroll
     for (int k = 1; k < MD_MAXC; ++k) r = c == k ? K.dtInv2m[k] : r;
+    return r;
+}
+__device__ __forceinline__ float kick_massf(const Kick& K, int c) {
+    float r = K.massf[0];
+#pragma unroll
+    for (int k = 1; k < MD_MAXC; ++k) r = c == k ? K.massf[k] : r;
     return r;
 }
 
@@ -1427,9 +1453,9 @@ __global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const 
             S.Lx[i] = L[0]; S.Ly[i] = L[1]; S.Lz[i] = L[2];
         }
         float4 p;
-        p.x = (float)(rx - origin[3 * i]);
-        p.y = (float)(ry - origin[3 * i + 1]);
-        p.z = (float)(rz - origin[3 * i + 2]);
+        p.x = d2f_int(rx - origin[3 * i]);
+        p.y = d2f_int(ry - origin[3 * i + 1]);
+        p.z = d2f_int(rz - origin[3 * i + 2]);
         const float4 q0 = xlref[i];
         p.w = q0.w;
         xlf[i] = p;
@@ -1502,11 +1528,16 @@ __global__ void k_post(State S, Kick K, double* partials, int pstride) {
 // molecule rotates (both half kicks use the same F): the same FP64
 // operations in the same order as k_post followed by k_pre, one pass over
 // the state instead of two.
+// With MIXED the kinetic-energy terms m v^2 are FP32 products of the
+// rounded velocities, summed per warp with compensation (FP64 from there on,
+// like the other global sums); the state update itself is FP64 either way.
+template <bool MIXED>
 __global__ void k_post_pre(State S, Kick K, double* partials, int pstride, float4* xlf, const double* origin,
                            const float4* xlref, unsigned* disp_max) {
     __shared__ float smax[8];
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double mv2 = 0.0;
+    float mv2f = 0.f;
     float d2 = 0.f;
     if (i < S.n) {
         const int ci = S.comp[i];
@@ -1515,27 +1546,31 @@ __global__ void k_post_pre(State S, Kick K, double* partials, int pstride, float
         const double dtInv2m = kick_dtInv2m(K, ci);
         const double F[3] = {S.Fx[i], S.Fy[i], S.Fz[i]};
         double v[3] = {S.vx[i], S.vy[i], S.vz[i]};
-        double v2 = 0.;
-        for (int d = 0; d < 3; ++d) {
-            v[d] += dtInv2m * F[d];
-            v2 += v[d] * v[d];
+        for (int d = 0; d < 3; ++d) v[d] += dtInv2m * F[d];
+        if (MIXED) {
+            const float vx = d2f_int(v[0]), vy = d2f_int(v[1]), vz = d2f_int(v[2]);
+            mv2f = kick_massf(K, ci) * (vx * vx + (vy * vy + vz * vz));
+        } else {
+            double v2 = 0.;
+            for (int d = 0; d < 3; ++d) v2 += v[d] * v[d];
+            mv2 = C.m * v2;
         }
-        mv2 = C.m * v2;
         for (int d = 0; d < 3; ++d) v[d] = v[d] + dtInv2m * F[d];
         const double rx = S.rx[i] + dt * v[0], ry = S.ry[i] + dt * v[1], rz = S.rz[i] + dt * v[2];
         S.vx[i] = v[0]; S.vy[i] = v[1]; S.vz[i] = v[2];
         S.rx[i] = rx; S.ry[i] = ry; S.rz[i] = rz;
         const float4 q0 = xlref[i];
         float4 p;
-        p.x = (float)(rx - origin[3 * i]);
-        p.y = (float)(ry - origin[3 * i + 1]);
-        p.z = (float)(rz - origin[3 * i + 2]);
+        p.x = d2f_int(rx - origin[3 * i]);
+        p.y = d2f_int(ry - origin[3 * i + 1]);
+        p.z = d2f_int(rz - origin[3 * i + 2]);
         p.w = q0.w;
         xlf[i] = p;
         const float ddx = p.x - q0.x, ddy = p.y - q0.y, ddz = p.z - q0.z;
         d2 = ddx * ddx + ddy * ddy + ddz * ddz;
     }
-    warp_partial(partials, pstride, 12, mv2);
+    if (MIXED) warp_partial_f32(partials, pstride, 12, mv2f);
+    else warp_partial(partials, pstride, 12, mv2);
     for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, o));
     if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = d2;
     __syncthreads();
