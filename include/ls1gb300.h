@@ -34,6 +34,13 @@
  *   md_integrate_post           Leapfrog::eventForcesCalculated (Leapfrog.cpp:32-36, 63-147)
  *   md_run                      the hot part of Simulation::simulateOneTimestep
  *                               (Simulation.cpp:1076-1300) for an NVE run
+ *   md_write_phasespace_binary  Domain::writeCheckpoint with the binary format
+ *                               (src/Domain.cpp:581-625, FullMolecule::writeBinary
+ *                               src/molecules/FullMolecule.cpp:448-470), as the
+ *                               CheckpointWriter's `binary` type calls it
+ *                               (src/io/CheckpointWriter.cpp:56-80)
+ *   md_read_phasespace_binary   BinaryReader::readPhaseSpaceHeader + readPhaseSpace
+ *                               (src/io/BinaryReader.cpp:76-343)
  */
 #ifndef LS1GB300_H
 #define LS1GB300_H
@@ -139,6 +146,18 @@ int md_upload_molecules(md_ctx* ctx, int64_t n, const uint64_t* id, const int32_
  * last force evaluation. */
 int md_download_molecules(md_ctx* ctx, int64_t n, uint64_t* id, int32_t* comp, double* r, double* v,
                           double* q, double* L, double* F, double* M, double* Vi);
+
+/* ls1's binary phase-space (checkpoint) files, packed and unpacked on the
+ * device.  Write: <prefix>.header.xml (time, box, molecule count, format
+ * ICRVQD) and <prefix>.dat, one 116-byte record per molecule in upload order
+ * (id u64, component u32 1-based, r[3] wrapped into the box, v[3], q[4]
+ * w,x,y,z, L[3], little-endian doubles).  Read: a header/data pair in the
+ * formats ICRVQD, ICRV or IRV replaces the context's molecules (components
+ * must be set; the header's box must equal the context's to 1e-14 relative);
+ * returns the header's time and the molecule count. */
+int md_write_phasespace_binary(md_ctx* ctx, const char* prefix, double time);
+int md_read_phasespace_binary(md_ctx* ctx, const char* header_path, const char* data_path, double* time,
+                              int64_t* n);
 
 int md_rebin_and_halo(md_ctx* ctx, md_bin_stats* stats);
 int md_get_cell_assignment(md_ctx* ctx, int64_t n, int64_t* cell);

@@ -65,6 +65,8 @@ def load_library(path: str = LIB_PATH):
     L.md_longrange_homogeneous.argtypes = [vp, i32, dp, dp]
     L.md_set_thermostat.argtypes = [vp, d, i32]
     L.md_apply_thermostat.argtypes = [vp, dp, dp]
+    L.md_write_phasespace_binary.argtypes = [vp, C.c_char_p, d]
+    L.md_read_phasespace_binary.argtypes = [vp, C.c_char_p, C.c_char_p, dp, C.POINTER(i64)]
     L.md_batch_create.argtypes = [C.POINTER(vp), C.POINTER(abi.MdBatchConfig)]
     L.md_batch_destroy.argtypes = [vp]
     L.md_batch_last_error.argtypes = [vp]
@@ -195,6 +197,30 @@ class Engine:
         self._check(self.L.md_longrange_homogeneous(self.h, int(add_to_molecule_virial), C.byref(u), C.byref(w)),
                     "md_longrange_homogeneous")
         return u.value, w.value
+
+    def write_phasespace_binary(self, prefix: str, time: float = 0.0):
+        """<prefix>.header.xml + <prefix>.dat in ls1's binary checkpoint format."""
+        self._check(self.L.md_write_phasespace_binary(self.h, os.fsencode(prefix), time), "md_write_phasespace_binary")
+
+    def read_phasespace_binary(self, header: str, data: str):
+        """Replace the molecules by those of a binary phase-space file pair; returns (time, n)."""
+        t, n = C.c_double(), C.c_int64()
+        self._check(self.L.md_read_phasespace_binary(self.h, os.fsencode(header), os.fsencode(data), C.byref(t),
+                                                     C.byref(n)), "md_read_phasespace_binary")
+        self.n = n.value
+        return t.value, n.value
+
+    def write_checkpoint(self, prefix: str, step: int, time: float, num_steps: int = 0, write_frequency: int = 1,
+                         incremental: bool = True) -> str:
+        """CheckpointWriter::endStep with the binary type (src/io/CheckpointWriter.cpp:56-80):
+        <prefix>[-<step / frequency, zero-padded>].restart{.header.xml,.dat}; returns the name."""
+        name = prefix
+        if incremental:
+            digits = int(np.ceil(np.log(float(num_steps // write_frequency)) / np.log(10.0))) if num_steps else 0
+            name += "-" + str(step // write_frequency).rjust(max(digits, 0), "0")
+        name += ".restart"
+        self.write_phasespace_binary(name, time)
+        return name
 
     def molecules(self) -> dict:
         n = self.n

@@ -135,3 +135,56 @@ class Oracle:
         lib().orc_get_molecules(self.h, n, *(out[k].ctypes.data for k in
                                              ("ids", "comp", "r", "v", "q", "L", "F", "M", "Vi")))
         return out
+
+
+# ---------------------------------------------------------------- binary phase space
+# ls1's binary checkpoint format, restated with numpy (test infrastructure:
+# the checker of the engine's device-side writer and reader).
+#   record (FullMolecule::writeBinary, src/molecules/FullMolecule.cpp:448-470):
+#     id u64, component u32 (1-based), r[3], v[3], q[4] (w, x, y, z), L[3]
+#     as little-endian doubles, 116 bytes packed;
+#   formats read by BinaryReader::readPhaseSpace (src/io/BinaryReader.cpp:186-226):
+#     ICRVQD as above, ICRV (no q, L: q = (1, 0, 0, 0), L = 0), IRV (no
+#     component either: component 1);
+#   header (Domain::writeCheckpointHeaderXML, src/Domain.cpp:581-605):
+#     <time>, <length>/<x|y|z> in "%21.15e", <number>, <format type="...">.
+RECORD_DTYPES = {
+    "ICRVQD": np.dtype([("id", "<u8"), ("cid", "<u4"), ("r", "<f8", 3), ("v", "<f8", 3), ("q", "<f8", 4),
+                        ("L", "<f8", 3)]),
+    "ICRV": np.dtype([("id", "<u8"), ("cid", "<u4"), ("r", "<f8", 3), ("v", "<f8", 3)]),
+    "IRV": np.dtype([("id", "<u8"), ("r", "<f8", 3), ("v", "<f8", 3)]),
+}
+
+
+def phasespace_binary_records(ids, comp, r, v, q, L) -> bytes:
+    """ICRVQD records of the given molecules in the given order (comp 0-based)."""
+    a = np.zeros(len(ids), RECORD_DTYPES["ICRVQD"])
+    a["id"] = ids
+    a["cid"] = np.asarray(comp) + 1
+    a["r"], a["v"], a["q"], a["L"] = r, v, q, L
+    return a.tobytes()
+
+
+def phasespace_binary_header(box, n, time) -> str:
+    """The header text Domain::writeCheckpointHeaderXML writes for one process."""
+    f = lambda x: "%21.15e" % x  # noqa: E731
+    return ("<?xml version='1.0' encoding='UTF-8'?>\n<mardyn version=\"20100525\" >\n\t<headerinfo>\n"
+            f"\t\t<time>{f(time)}</time>\n\t\t<length>\n"
+            f"\t\t\t<x>{f(box[0])}</x> <y>{f(box[1])}</y> <z>{f(box[2])}</z>\n\t\t</length>\n"
+            f"\t\t<number>{int(n)}</number>\n\t\t<format type=\"ICRVQD\"/>\n\t</headerinfo>\n</mardyn>\n")
+
+
+def read_phasespace_binary(header_text: str, data: bytes):
+    """(time, box, dict of arrays in file order, comp 0-based) of a header and data pair."""
+    import re
+    get = lambda tag: re.search(r"<%s>\s*([^<]+?)\s*</%s>" % (tag, tag), header_text).group(1)  # noqa: E731
+    time = float(get("time"))
+    box = np.array([float(get("x")), float(get("y")), float(get("z"))])
+    n = int(get("number"))
+    fmt = re.search(r"<format\s+type=\"([A-Z]+)\"", header_text).group(1)
+    a = np.frombuffer(data, RECORD_DTYPES[fmt], count=n)
+    out = {"id": a["id"].copy(), "r": a["r"].copy(), "v": a["v"].copy()}
+    out["comp"] = (a["cid"].astype(np.int64) - 1) if "cid" in a.dtype.names else np.zeros(n, np.int64)
+    out["q"] = a["q"].copy() if "q" in a.dtype.names else np.tile([1.0, 0.0, 0.0, 0.0], (n, 1))
+    out["L"] = a["L"].copy() if "L" in a.dtype.names else np.zeros((n, 3))
+    return time, box, out

@@ -21,6 +21,14 @@
 //       The homogeneous long-range correction (longRange/Homogeneous): init +
 //       calculateLongRange, then the global values with zero local Upot and
 //       virial, so the printed global Upot and virial are the corrections.
+//   binw <file.inp> <rc> <prefix> <time>
+//       Domain::writeCheckpoint with the binary format (the CheckpointWriter's
+//       `binary` type): <prefix>.header.xml (writeCheckpointHeaderXML) and
+//       <prefix>.dat (FullMolecule::writeBinary of every molecule in container
+//       order).
+//   binr <components.inp> <header.xml> <data> <rc>
+//       Components and box from the ASCII file's header, then BinaryReader:
+//       readPhaseSpaceHeader + readPhaseSpace; prints the molecules read.
 //   steps <file.inp> <rc> <rcLJ> <dt> <nsteps>
 //       NVE Leapfrog steps with the periodic halo, in the order of the
 //       reference's Simulation::simulateOneTimestep (thermostat off, no
@@ -83,6 +91,7 @@
 #include "ensemble/EnsembleBase.h"
 #include "integrators/Leapfrog.h"
 #include "io/ASCIIReader.h"
+#include "io/BinaryReader.h"
 #include "longRange/Homogeneous.h"
 #include "thermostats/VelocityScalingThermostat.h"
 #include "molecules/Molecule.h"
@@ -257,6 +266,40 @@ int runLrc(const std::string& file, double rc, double rcLJ) {
 	return 0;
 }
 
+int runBinWrite(const std::string& file, double rc, const std::string& prefix, double time) {
+	Setup s;
+	load(s, file, rc, rc);
+	s.domain->writeCheckpoint(prefix, s.lc, s.dd, time, true);
+	std::printf("N %lu\n", s.domain->getglobalNumMolecules(true, s.lc, s.dd));
+	return 0;
+}
+
+int runBinRead(const std::string& inp, const std::string& header, const std::string& data, double rc) {
+	Setup s;
+	new Simulation();
+	s.domain = global_simulation->getDomain();
+	s.dd = &global_simulation->domainDecomposition();
+	global_simulation->setcutoffRadius(rc);
+	global_simulation->setLJCutoff(rc);
+	s.reader.setPhaseSpaceHeaderFile(inp);
+	s.reader.readPhaseSpaceHeader(s.domain, 1.0);
+	BinaryReader br;
+	br.setPhaseSpaceHeaderFile(header);
+	br.setPhaseSpaceFile(data);
+	br.readPhaseSpaceHeader(s.domain, 1.0);
+	double bmin[3], bmax[3];
+	for (int d = 0; d < 3; ++d) {
+		bmin[d] = s.dd->getBoundingBoxMin(d, s.domain);
+		bmax[d] = s.dd->getBoundingBoxMax(d, s.domain);
+	}
+	s.lc = new LinkedCells(bmin, bmax, rc);
+	br.readPhaseSpace(s.lc, s.domain, s.dd);
+	std::printf("TIME %.17g\nLENGTH %.17g %.17g %.17g\n", global_simulation->getSimulationTime(),
+				s.domain->getGlobalLength(0), s.domain->getGlobalLength(1), s.domain->getGlobalLength(2));
+	printMolecules(s);
+	return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -270,8 +313,12 @@ int main(int argc, char** argv) {
 						std::atof(argv[7]));
 	if (argc >= 5 && std::string(argv[1]) == "lrc")
 		return runLrc(argv[2], std::atof(argv[3]), std::atof(argv[4]));
+	if (argc >= 6 && std::string(argv[1]) == "binw")
+		return runBinWrite(argv[2], std::atof(argv[3]), argv[4], std::atof(argv[5]));
+	if (argc >= 6 && std::string(argv[1]) == "binr")
+		return runBinRead(argv[2], argv[3], argv[4], std::atof(argv[5]));
 	if (argc >= 7 && std::string(argv[1]) == "steps")
 		return runSteps(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]));
-	std::fprintf(stderr, "usage: %s forces <inp> <rc> <rcLJ> <periodic> | lrc <inp> <rc> <rcLJ> | steps <inp> <rc> <rcLJ> <dt> <n> | nvt <inp> <rc> <rcLJ> <dt> <n> <T>\n", argv[0]);
+	std::fprintf(stderr, "usage: %s forces <inp> <rc> <rcLJ> <periodic> | lrc <inp> <rc> <rcLJ> | steps <inp> <rc> <rcLJ> <dt> <n> | nvt <inp> <rc> <rcLJ> <dt> <n> <T> | binw <inp> <rc> <prefix> <time> | binr <inp> <header> <data> <rc>\n", argv[0]);
 	return 2;
 }
