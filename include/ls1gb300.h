@@ -41,6 +41,8 @@
  *                               (src/io/CheckpointWriter.cpp:56-80)
  *   md_read_phasespace_binary   BinaryReader::readPhaseSpaceHeader + readPhaseSpace
  *                               (src/io/BinaryReader.cpp:76-343)
+ *   md_planar_init/apply        Planar::init / calculateLongRange
+ *                               (src/longRange/Planar.cpp:38-157, 223-460)
  */
 #ifndef LS1GB300_H
 #define LS1GB300_H
@@ -158,6 +160,26 @@ int md_download_molecules(md_ctx* ctx, int64_t n, uint64_t* id, int32_t* comp, d
 int md_write_phasespace_binary(md_ctx* ctx, const char* prefix, double time);
 int md_read_phasespace_binary(md_ctx* ctx, const char* header_path, const char* data_path, double* time,
                               int64_t* n);
+
+/* Planar long-range correction for planar interfaces normal to y
+ * (longRange/Planar.cpp, `<longrange type="planar">`).  md_planar_apply is
+ * called after each md_compute_forces, where the reference calls
+ * Planar::calculateLongRange (before calcFM): every `frequency` calls (the
+ * first included) it samples the density profiles of the LJ centres and
+ * dipolar components over `slabs` slabs and recomputes the slab corrections;
+ * every call it adds each LJ centre's slab force to the y force (and its
+ * torque) of molecules with y in [region_lo, region_hi], the slab virial to
+ * every molecule's virial, and returns UpotCorr and VirialCorr (the values
+ * the reference hands to Domain::setUpotCorr / setVirialCorr). */
+typedef struct {
+    int32_t slabs;             /* <slabs>                                                */
+    int32_t frequency;         /* <frequency>: profile and corrections every n-th call   */
+    double region_lo;          /* <region><left>: force corrections for y >= region_lo   */
+    double region_hi;          /* <region><right>: ... and y <= region_hi (box: L_y)     */
+    double target_temperature; /* thermostat-0 target temperature (dipole corrections)   */
+} md_planar_config;
+int md_planar_init(md_ctx* ctx, const md_planar_config* cfg);
+int md_planar_apply(md_ctx* ctx, double* upot_corr, double* virial_corr);
 
 int md_rebin_and_halo(md_ctx* ctx, md_bin_stats* stats);
 int md_get_cell_assignment(md_ctx* ctx, int64_t n, int64_t* cell);

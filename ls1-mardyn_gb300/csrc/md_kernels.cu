@@ -1583,4 +1583,5 @@ __global__ void k_post_pre(State S, Kick K, double* partials, int pstride, float
 
 #include "md_adjoint.inc"
 #include "md_api.inc"
+#include "md_planar.inc"
 #include "md_batch.inc"

@@ -60,6 +60,11 @@ class MdKineticOut(C.Structure):
     _fields_ = [("summv2", C.c_double), ("sumIw2", C.c_double), ("n", C.c_int64), ("rot_dof", C.c_int64)]
 
 
+class MdPlanarConfig(C.Structure):
+    _fields_ = [("slabs", C.c_int32), ("frequency", C.c_int32), ("region_lo", C.c_double), ("region_hi", C.c_double),
+                ("target_temperature", C.c_double)]
+
+
 class MdStepRecord(C.Structure):
     _fields_ = [("upot", C.c_double), ("virial", C.c_double), ("summv2", C.c_double), ("sumIw2", C.c_double)]
 

@@ -65,6 +65,8 @@ def load_library(path: str = LIB_PATH):
     L.md_longrange_homogeneous.argtypes = [vp, i32, dp, dp]
     L.md_set_thermostat.argtypes = [vp, d, i32]
     L.md_apply_thermostat.argtypes = [vp, dp, dp]
+    L.md_planar_init.argtypes = [vp, C.POINTER(abi.MdPlanarConfig)]
+    L.md_planar_apply.argtypes = [vp, dp, dp]
     L.md_write_phasespace_binary.argtypes = [vp, C.c_char_p, d]
     L.md_read_phasespace_binary.argtypes = [vp, C.c_char_p, C.c_char_p, dp, C.POINTER(i64)]
     L.md_batch_create.argtypes = [C.POINTER(vp), C.POINTER(abi.MdBatchConfig)]
@@ -196,6 +198,21 @@ class Engine:
         u, w = C.c_double(), C.c_double()
         self._check(self.L.md_longrange_homogeneous(self.h, int(add_to_molecule_virial), C.byref(u), C.byref(w)),
                     "md_longrange_homogeneous")
+        return u.value, w.value
+
+    def planar_init(self, slabs: int, frequency: int = 10, region: Optional[Sequence[float]] = None,
+                    target_temperature: Optional[float] = None):
+        """Planar long-range correction (longRange/Planar): slabs along y, profiles every `frequency` calls,
+        force corrections in the y range `region` (default: the whole box)."""
+        lo, hi = (0.0, float(self.ps.box[1])) if region is None else region
+        T = float(self.ps.temperature) if target_temperature is None else target_temperature
+        cfg = abi.MdPlanarConfig(int(slabs), int(frequency), float(lo), float(hi), T)
+        self._check(self.L.md_planar_init(self.h, C.byref(cfg)), "md_planar_init")
+
+    def planar_apply(self):
+        """(UpotCorr, VirialCorr) of this call; adds the corrections to F, M and Vi."""
+        u, w = C.c_double(), C.c_double()
+        self._check(self.L.md_planar_apply(self.h, C.byref(u), C.byref(w)), "md_planar_apply")
         return u.value, w.value
 
     def write_phasespace_binary(self, prefix: str, time: float = 0.0):

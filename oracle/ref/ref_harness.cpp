@@ -29,6 +29,12 @@
 //   binr <components.inp> <header.xml> <data> <rc>
 //       Components and box from the ASCII file's header, then BinaryReader:
 //       readPhaseSpaceHeader + readPhaseSpace; prints the molecules read.
+//   planar <file.inp> <rc> <rcLJ> <dt> <nsteps> <slabs> <frequency> <y_lo> <y_hi>
+//       As `steps`, with the planar long-range correction (longRange/Planar)
+//       in the place Simulation gives it: after the traversal and before
+//       calcFM, at the first force evaluation and in every step; force
+//       corrections applied to molecules with y in [y_lo, y_hi].  LRC
+//       records carry the step's UpotCorr and VirialCorr.
 //   steps <file.inp> <rc> <rcLJ> <dt> <nsteps>
 //       NVE Leapfrog steps with the periodic halo, in the order of the
 //       reference's Simulation::simulateOneTimestep (thermostat off, no
@@ -86,8 +92,9 @@
 #include <omp.h>
 #define private public
 #include "Simulation.h"
-#undef private
 #include "Domain.h"
+#include "longRange/Planar.h"
+#undef private
 #include "ensemble/EnsembleBase.h"
 #include "integrators/Leapfrog.h"
 #include "io/ASCIIReader.h"
@@ -249,6 +256,49 @@ int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nst
 	return 0;
 }
 
+int runPlanar(const std::string& file, double rc, double rcLJ, double dt, int nsteps, int slabs, int freq,
+			  double ylo, double yhi) {
+	Setup s;
+	load(s, file, rc, rcLJ);
+	s.domain->thermostatOff();
+	s.dd->exchangeMolecules(s.lc, s.domain);
+	s.lc->updateMoleculeCaches();
+	s.domain->initParameterStreams(rc, rcLJ);
+	global_simulation->_moleculeContainer = s.lc;
+	VectorizedCellProcessor vcp(*s.domain, rc, rcLJ);
+	Leapfrog integrator(dt);
+	Planar lrc(rc, rcLJ, s.domain, s.dd, s.lc, (unsigned)slabs, global_simulation);
+	lrc.frequency = freq;
+	lrc._region.refPosID[0] = lrc._region.refPosID[1] = 0;
+	lrc._region.refPos[0] = lrc._region.actPos[0] = ylo;
+	lrc._region.refPos[1] = lrc._region.actPos[1] = yhi;
+	lrc.init();
+	auto forcesWithLrc = [&]() {
+		s.lc->traverseCells(vcp);
+		lrc.calculateLongRange();
+		for (auto m = s.lc->iterator(ParticleIterator::ALL_CELLS); m.isValid(); ++m) m->calcFM();
+		s.lc->deleteOuterParticles();
+		std::printf("LRC %.17g %.17g\n", s.domain->_UpotCorr, s.domain->_VirialCorr);
+	};
+	forcesWithLrc();
+	std::printf("STEP 0 %.17g %.17g nan nan\n", s.domain->getLocalUpot(), s.domain->getLocalVirial());
+	for (int k = 1; k <= nsteps; ++k) {
+		integrator.eventNewTimestep(s.lc, s.domain);
+		s.lc->update();
+		s.dd->exchangeMolecules(s.lc, s.domain);
+		s.lc->updateMoleculeCaches();
+		forcesWithLrc();
+		integrator.eventForcesCalculated(s.lc, s.domain);
+		const double upot = s.domain->getLocalUpot();
+		const double vir = s.domain->getLocalVirial();
+		s.domain->calculateGlobalValues(s.dd, s.lc, false, 1.0);
+		std::printf("STEP %d %.17g %.17g %.17g %.17g\n", k, upot, vir, 2.0 * s.domain->getGlobalUkinTrans(),
+					2.0 * s.domain->getGlobalUkinRot());
+	}
+	printMolecules(s);
+	return 0;
+}
+
 int runLrc(const std::string& file, double rc, double rcLJ) {
 	Setup s;
 	load(s, file, rc, rcLJ);
@@ -313,6 +363,9 @@ int main(int argc, char** argv) {
 						std::atof(argv[7]));
 	if (argc >= 5 && std::string(argv[1]) == "lrc")
 		return runLrc(argv[2], std::atof(argv[3]), std::atof(argv[4]));
+	if (argc >= 11 && std::string(argv[1]) == "planar")
+		return runPlanar(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]),
+						 std::atoi(argv[7]), std::atoi(argv[8]), std::atof(argv[9]), std::atof(argv[10]));
 	if (argc >= 6 && std::string(argv[1]) == "binw")
 		return runBinWrite(argv[2], std::atof(argv[3]), argv[4], std::atof(argv[5]));
 	if (argc >= 6 && std::string(argv[1]) == "binr")
