@@ -257,6 +257,20 @@ int md_longrange_homogeneous(md_ctx* ctx, int32_t add_to_molecule_virial, double
 int md_set_thermostat(md_ctx* ctx, double target_temperature, int32_t explosion_heuristics);
 int md_apply_thermostat(md_ctx* ctx, double* beta_trans, double* beta_rot);
 
+/* Component-wise velocity-scaling thermostats (Domain::setComponentThermostat /
+ * setTargetTemperature with ids >= 1, Domain::calculateGlobalValues and
+ * VelocityScalingThermostat::apply with several thermostats): component c is
+ * on thermostat component_thermostat[c] (1..nthermostats; every component
+ * needs one), thermostat t has target target_temperatures[t - 1]; betas per
+ * thermostat from its own sums, the explosion heuristic per thermostat with
+ * counters shared as in the reference.  Replaces a global thermostat;
+ * md_run and md_apply_thermostat then scale each molecule with its
+ * thermostat's betas.  md_thermostat_betas reads the betas of the last
+ * application (thermostat 0 = the global one). */
+int md_set_thermostats(md_ctx* ctx, const int32_t* component_thermostat, int32_t nthermostats,
+                       const double* target_temperatures, int32_t explosion_heuristics);
+int md_thermostat_betas(md_ctx* ctx, int32_t thermostat, double* beta_trans, double* beta_rot);
+
 /* Wait for all work of the context. */
 int md_sync(md_ctx* ctx);
 

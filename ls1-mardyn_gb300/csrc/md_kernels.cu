@@ -53,8 +53,11 @@ struct Scratch {
     int* list_need;         // max candidates needed (overflow report)
 };
 
-#define NPART 16   // partial-sum slots per block
+#define NPART 32   // partial-sum slots per block
 // slots: 0 upot6lj 1 upotXpoles 2 virial 3 myRF 4 mol_pairs 5..11 site pairs 12 summv2 13 sumIw2 14 n 15 rotdof
+// 16..23 summv2 per component, 24..31 sumIw2 per component (component-wise thermostats only)
+#define SLOT_MV2_C 16
+#define SLOT_IW2_C 24
 
 // ------------------------------------------------------------------ reductions
 // Every kernel that contributes to the global sums writes, per warp of its
@@ -174,14 +177,21 @@ __device__ double block_sum(double v, double* sh) {
 }
 
 // slots 0..11 come from the force kernel (nw_force warps), 12..13 from the
-// post-force half step (nw_post warps); a count of 0 leaves a slot at 0.
-// Stage 1: FIN_SEG blocks per slot each sum a contiguous segment; stage 2
-// sums the FIN_SEG segment sums of each slot in order (deterministic).
+// post-force half step (nw_post warps), 16..31 from the post-force half step
+// when it writes per-component sums (nw_comp warps); a count of 0 leaves a
+// slot at 0.  Stage 1: FIN_SEG blocks per slot each sum a contiguous
+// segment; stage 2 sums the FIN_SEG segment sums of each slot in order
+// (deterministic).
 #define FIN_SEG 64
-__global__ void k_finalize1(const double* partials, int pstride, int nw_force, int nw_post, int nw_rot, double* seg) {
+__global__ void k_finalize1(const double* partials, int pstride, int nw_force, int nw_post, int nw_rot, int nw_comp,
+                            double* seg) {
     __shared__ double sh[32];
     const int s = blockIdx.y, b = blockIdx.x;
-    const int nw = s < 12 ? nw_force : (s == 12 ? nw_post : (s == 13 ? nw_rot : 0));
+    const int nw = s < 12 ? nw_force : (s == 12 ? nw_post : (s == 13 ? nw_rot : (s >= SLOT_MV2_C ? nw_comp : 0)));
+    if (nw == 0) {  // slot unused by this step (whole block leaves together)
+        if (threadIdx.x == 0) seg[s * FIN_SEG + b] = 0.0;
+        return;
+    }
     const int per = (nw + FIN_SEG - 1) / FIN_SEG;
     const int lo = b * per, hi = min(nw, lo + per);
     double v = 0.0;
@@ -1492,7 +1502,7 @@ __global__ void k_sum_int(const int* a, int64_t n, unsigned long long* out) {
 }
 
 // FullMolecule::upd_postF with the Leapfrog sums.
-__global__ void k_post(State S, Kick K, double* partials, int pstride) {
+__global__ void k_post(State S, Kick K, double* partials, int pstride, int percomp) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double mv2 = 0.0, iw2 = 0.0;
     if (i < S.n) {
@@ -1522,6 +1532,13 @@ __global__ void k_post(State S, Kick K, double* partials, int pstride) {
     }
     warp_partial(partials, pstride, 12, mv2);
     if (cP.any_rotation) warp_partial(partials, pstride, 13, iw2);
+    if (percomp) {  // per-component sums for component-wise thermostats
+        const int c = i < S.n ? S.comp[i] : -1;
+        for (int q = 0; q < percomp; ++q) {
+            warp_partial(partials, pstride, SLOT_MV2_C + q, c == q ? mv2 : 0.0);
+            warp_partial(partials, pstride, SLOT_IW2_C + q, c == q ? iw2 : 0.0);
+        }
+    }
 }
 
 // upd_postF of step k fused with upd_preF of step k + 1 for systems where no

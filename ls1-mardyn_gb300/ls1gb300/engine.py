@@ -65,6 +65,8 @@ def load_library(path: str = LIB_PATH):
     L.md_longrange_homogeneous.argtypes = [vp, i32, dp, dp]
     L.md_set_thermostat.argtypes = [vp, d, i32]
     L.md_apply_thermostat.argtypes = [vp, dp, dp]
+    L.md_set_thermostats.argtypes = [vp, vp, i32, dp, i32]
+    L.md_thermostat_betas.argtypes = [vp, i32, dp, dp]
     L.md_planar_init.argtypes = [vp, C.POINTER(abi.MdPlanarConfig)]
     L.md_planar_apply.argtypes = [vp, dp, dp]
     L.md_write_phasespace_binary.argtypes = [vp, C.c_char_p, d]
@@ -186,6 +188,21 @@ class Engine:
         """Global velocity-scaling thermostat at the target (<= 0: NVE), applied by run()."""
         self._check(self.L.md_set_thermostat(self.h, float(target_temperature), int(explosion_heuristics)),
                     "md_set_thermostat")
+
+    def set_thermostats(self, component_thermostat: Sequence[int], targets: Sequence[float],
+                        explosion_heuristics: bool = True):
+        """Component-wise thermostats: component c on thermostat component_thermostat[c] (ids from 1),
+        thermostat t at target targets[t - 1]."""
+        m = np.ascontiguousarray(component_thermostat, np.int32)
+        t = np.ascontiguousarray(targets, np.float64)
+        self._check(self.L.md_set_thermostats(self.h, m.ctypes.data, len(t), abi.dptr(t), int(explosion_heuristics)),
+                    "md_set_thermostats")
+
+    def thermostat_betas(self, thermostat: int = 0):
+        bt, br = C.c_double(), C.c_double()
+        self._check(self.L.md_thermostat_betas(self.h, int(thermostat), C.byref(bt), C.byref(br)),
+                    "md_thermostat_betas")
+        return bt.value, br.value
 
     def apply_thermostat(self):
         """One thermostat application after post(); returns (beta_trans, beta_rot)."""

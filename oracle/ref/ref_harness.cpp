@@ -17,6 +17,12 @@
 //       D *= beta_rot (Simulation::simulateOneTimestep, VELSCALE_THERMOSTAT
 //       with one thermostat).  STEP records carry the values before scaling
 //       and a BETA record follows each.
+//   nvtc <file.inp> <rc> <rcLJ> <dt> <nsteps> <T_1> ... <T_ncomp>
+//       As `nvt` with a component-wise thermostat: component c on thermostat
+//       c+1 with target T_{c+1} (Domain::setComponentThermostat /
+//       setTargetTemperature), the velocity scaling of
+//       Simulation::simulateOneTimestep's several-thermostats branch.  BETA
+//       records carry <k> <thermostat> <beta_trans> <beta_rot>.
 //   lrc <file.inp> <rc> <rcLJ>
 //       The homogeneous long-range correction (longRange/Homogeneous): init +
 //       calculateLongRange, then the global values with zero local Upot and
@@ -299,6 +305,51 @@ int runPlanar(const std::string& file, double rc, double rcLJ, double dt, int ns
 	return 0;
 }
 
+int runNvtComponentwise(const std::string& file, double rc, double rcLJ, double dt, int nsteps,
+						const std::vector<double>& T) {
+	Setup s;
+	load(s, file, rc, rcLJ);
+	s.domain->thermostatOn();
+	const int ncomp = (int)global_simulation->getEnsemble()->getComponents()->size();
+	for (int c = 0; c < ncomp; ++c) s.domain->setComponentThermostat(c, c + 1);
+	for (int c = 0; c < ncomp; ++c) s.domain->setTargetTemperature(c + 1, T[c]);
+	VelocityScalingThermostat thermostat;
+	s.dd->exchangeMolecules(s.lc, s.domain);
+	s.lc->updateMoleculeCaches();
+	s.domain->initParameterStreams(rc, rcLJ);
+	VectorizedCellProcessor vcp(*s.domain, rc, rcLJ);
+	Leapfrog integrator(dt);
+	forceStep(s, vcp);
+	std::printf("STEP 0 %.17g %.17g nan nan\n", s.domain->getLocalUpot(), s.domain->getLocalVirial());
+	for (int k = 1; k <= nsteps; ++k) {
+		integrator.eventNewTimestep(s.lc, s.domain);
+		s.lc->update();
+		s.dd->exchangeMolecules(s.lc, s.domain);
+		s.lc->updateMoleculeCaches();
+		forceStep(s, vcp);
+		integrator.eventForcesCalculated(s.lc, s.domain);
+		const double upot = s.domain->getLocalUpot();
+		const double vir = s.domain->getLocalVirial();
+		s.domain->calculateGlobalValues(s.dd, s.lc, false, 1.0);
+		std::printf("STEP %d %.17g %.17g %.17g %.17g\n", k, upot, vir, 2.0 * s.domain->getGlobalUkinTrans(),
+					2.0 * s.domain->getGlobalUkinRot());
+		thermostat.enableComponentwise();
+		for (int c = 0; c < ncomp; ++c) {
+			const int tid = s.domain->getThermostat(c);
+			thermostat.setBetaTrans(tid, s.domain->getGlobalBetaTrans(tid));
+			thermostat.setBetaRot(tid, s.domain->getGlobalBetaRot(tid));
+			double v[3];
+			for (int d = 0; d < 3; d++) v[d] = s.domain->getThermostatDirectedVelocity(tid, d);
+			thermostat.setVelocity(tid, v);
+			std::printf("BETA %d %d %.17g %.17g\n", k, tid, s.domain->getGlobalBetaTrans(tid),
+						s.domain->getGlobalBetaRot(tid));
+		}
+		thermostat.apply(s.lc);
+	}
+	printMolecules(s);
+	return 0;
+}
+
 int runLrc(const std::string& file, double rc, double rcLJ) {
 	Setup s;
 	load(s, file, rc, rcLJ);
@@ -361,6 +412,12 @@ int main(int argc, char** argv) {
 	if (argc >= 8 && std::string(argv[1]) == "nvt")
 		return runSteps(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]),
 						std::atof(argv[7]));
+	if (argc >= 8 && std::string(argv[1]) == "nvtc") {
+		std::vector<double> T;
+		for (int a = 7; a < argc; ++a) T.push_back(std::atof(argv[a]));
+		return runNvtComponentwise(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]),
+								   std::atoi(argv[6]), T);
+	}
 	if (argc >= 5 && std::string(argv[1]) == "lrc")
 		return runLrc(argv[2], std::atof(argv[3]), std::atof(argv[4]));
 	if (argc >= 11 && std::string(argv[1]) == "planar")

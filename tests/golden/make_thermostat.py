@@ -39,5 +39,41 @@ def main():
         np.savez_compressed(os.path.join(HERE, "nvtt_" + name + ".npz"), **z)
 
 
+def two_component_lj(seed):
+    """1CLJ fcc 5^3x4 at rho* = 0.8 with every second molecule of a heavier,
+    smaller second component (m = 2, eps = 0.9, sigma = 0.95; LB mixing)."""
+    ps = mg.jitter(mg.psm.lj_fcc(5, 0.8, 1.0, seed=seed), 0.1, seed + 1)
+    ps.components = [mg.psm.one_center_lj(), mg.psm.one_center_lj(eps=0.9, sigma=0.95, m=2.0)]
+    ps.mixing = [(1.0, 1.0)]
+    ps.comp = (np.arange(ps.n) % 2).astype(np.int32)
+    return ps
+
+
+def main_componentwise():
+    """nvtc_*.npz: component c on thermostat c + 1 (oracle/ref/ref_harness.cpp `nvtc`); betas per step and
+    thermostat in `betas_c` rows (step, thermostat, beta_trans, beta_rot)."""
+    tmp = mg.tempfile.mkdtemp()
+    cases = [("lj2c", two_component_lj(21), 2.5, 2.5, 0.002, 20, (1.2, 0.8)),
+             ("mix500", mg.psm.mixture(500, 18.0, 500.0, seed=31), 1.0, 1.0, 9.118e-5, 10, (520.0, 480.0))]
+    for name, ps, rc, rclj, dt, n, T in cases:
+        path = os.path.join(tmp, name + ".inp")
+        mg.psm.write_inp(ps, path)
+        ps = mg.psm.read_inp(path)
+        p = mg.subprocess.run([mg.HARNESS, "nvtc", path, str(rc), str(rclj), str(dt), str(n)] + [str(x) for x in T],
+                              capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(p.stderr[-2000:])
+        res = mg.parse(p.stdout)
+        res["grid"] = np.zeros(3, np.int64)
+        res["cell_length"] = np.zeros(3)
+        betas = np.array([[float(x) for x in l.split()[1:]] for l in p.stdout.splitlines() if l.startswith("BETA")])
+        mg.store("nvtc_" + name, ps, rc, rclj, True, res, dt, n, True)
+        z = dict(np.load(os.path.join(HERE, "nvtc_" + name + ".npz")))
+        z["betas_c"] = betas
+        z["targets"] = np.array(T)
+        np.savez_compressed(os.path.join(HERE, "nvtc_" + name + ".npz"), **z)
+
+
 if __name__ == "__main__":
     main()
+    main_componentwise()

@@ -72,3 +72,43 @@ def test_step_by_step_thermostat_equals_md_run(engine_mod):
     assert ra.shape == (8, 4)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("name", golden_io.names("nvtc_"))
+def test_componentwise_thermostats_match_reference(engine_mod, name):
+    """Component c on thermostat c + 1 (tests/golden/nvtc_*.npz, the
+    reference's several-thermostats path): per-step Upot and virial of md_run
+    to 1e-8, final state to 1e-7; step by step, the betas of every thermostat
+    to 1e-10 against the reference's."""
+    ps, g = golden_io.load(name)
+    dt, n = float(g["dt"]), int(g["nsteps"])
+    targets = [float(x) for x in g["targets"]]
+    ids = list(range(1, len(targets) + 1))
+    a = engine_mod.Engine(ps, g["rc"], g["rc_lj"], precision="fp64")
+    a.set_thermostats(ids, targets)
+    a.forces()
+    rec = a.run(dt, n)
+    ref = g["steps"][1:, 1:]
+    for col in range(2):  # the reference's kinetic columns hold the last thermostat's sums
+        assert np.abs(rec[:, col] - ref[:, col]).max() <= 1e-8 * np.abs(ref[:, col]).max(), col
+    m = a.molecules()
+    a.close()
+    i, j = _by_id(m["ids"]), _by_id(g["out_ids"])
+    for key, gk in (("r", "out_r"), ("v", "out_v"), ("L", "out_L")):
+        assert np.abs(m[key][i] - g[gk][j]).max() <= 1e-7 * max(np.abs(g[gk]).max(), 1.0), key
+    b = engine_mod.Engine(ps, g["rc"], g["rc_lj"], precision="fp64")
+    b.set_thermostats(ids, targets)
+    b.forces()
+    got = []
+    for k in range(1, n + 1):
+        b.pre(dt)
+        b.forces()
+        b.post(dt)
+        b.apply_thermostat()
+        for t in ids:
+            got.append((k, t) + b.thermostat_betas(t))
+    b.close()
+    want = g["betas_c"]
+    got = np.array(got)
+    assert np.array_equal(got[:, :2], want[:, :2])
+    assert np.allclose(got[:, 2:], want[:, 2:], rtol=1e-10, atol=0)
