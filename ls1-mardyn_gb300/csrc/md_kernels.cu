@@ -1268,6 +1268,9 @@ __device__ __forceinline__ void warp_partial_acc(double* partials, int pstride, 
 
 #define MS_WARPS 4     // warps per block of the multi-site kernels
 #define MS_MOLS 32     // molecules per warp, one after another
+#ifndef MS_MIN_BLOCKS
+#define MS_MIN_BLOCKS 5  // FP32 variants: blocks per SM the register budget is sized for (96 registers, no spills)
+#endif
 
 // General multi-site molecules: all site pairs of every molecule pair inside
 // the molecule-centre cut-off (rc_lj for LJ centres, rc for the multipoles),
@@ -1275,7 +1278,7 @@ __device__ __forceinline__ void warp_partial_acc(double* partials, int pstride, 
 // Vi = 1/2 sum m_d o f.  Per lane the sums are compensated (FP32) or plain
 // (FP64); per molecule the 32 lanes are combined in FP64 in a fixed order.
 template <typename Real>
-__global__ void __launch_bounds__(MS_WARPS * 32) k_force_ms(State S, const float4* xlf, const Real* sd, const Real* se,
+__global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOCKS : 3) k_force_ms(State S, const float4* xlf, const Real* sd, const Real* se,
                                                             int stride, const uint32_t* nbr, const int* nnb, int maxnb,
                                                             double* partials, int pstride) {
     __shared__ Real soff[27][3];
