@@ -222,9 +222,18 @@ def max_over_ranks(pg, x: float) -> float:
     if pg is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if os.environ.get("BENCH_BACKEND", "nccl") == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     pg.all_reduce(t, op=pg.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(pg, world: int, n_per_rank: int, steps: int, ms_local: float):
+    """Whole-job molecule-updates/s of `world` independent replicas (one box
+    per rank, no collective on the data path): the updates of all ranks over
+    the slowest rank's timed region.  Returns (value, slowest ms)."""
+    ms = max_over_ranks(pg, ms_local)
+    return world * n_per_rank * steps / (ms * 1e-3), ms
 
 
 def run_reference(a, rank):
@@ -286,8 +295,7 @@ def run_batch(a, rank, world, local, pg):
     ms = cu.elapsed_ms(e0, e1)
     clocks = clock.stop()
     rebuilds = bt.rebuilds()
-    ms = max_over_ranks(pg, ms)
-    value = world * n * a.steps / (ms * 1e-3)
+    value, ms = replica_throughput(pg, world, n, a.steps, ms)
     # per-box errors of the mixed batch at its final state: Upot and pressure
     # p = (sum m v^2 + virial) / (3 V) from the last step's record against the
     # FP64 forces of the same positions
@@ -492,8 +500,7 @@ def main():
     cu.record(e1, stream)
     ms = cu.elapsed_ms(e0, e1)
     clocks = t_clock.stop()
-    ms = max_over_ranks(pg, ms)
-    value = world * n * a.steps / (ms * 1e-3)
+    value, ms = replica_throughput(pg, world, n, a.steps, ms)
     # per-kernel times on the engine stream, right after the timed region
     fo = eng.forces()
     kt = eng.time_kernels(5)
