@@ -198,6 +198,8 @@ def parse():
     ap.add_argument("--skin", type=float, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--integrator", default="leapfrog", choices=["leapfrog", "rmm"],
+                    help="rmm: the reduced memory mode (LeapfrogRMM + VCP1CLJRMM, 1CLJ only)")
     return ap.parse_args()
 
 
@@ -288,6 +290,7 @@ def run_batch(a, rank, world, local, pg):
     clock = ClockSampler(local)
     barrier(pg)
     e0, e1 = cu.event(), cu.event()
+    rb0 = bt.rebuilds()
     clock.start()
     cu.record(e0, stream)
     rec = bt.run(dt, a.steps, graph_steps=100, record=True)
@@ -295,6 +298,7 @@ def run_batch(a, rank, world, local, pg):
     ms = cu.elapsed_ms(e0, e1)
     clocks = clock.stop()
     rebuilds = bt.rebuilds()
+    rebuilds_timed = rebuilds - rb0
     value, ms = replica_throughput(pg, world, n, a.steps, ms)
     # per-box errors of the mixed batch at its final state: Upot and pressure
     # p = (sum m v^2 + virial) / (3 V) from the last step's record against the
@@ -351,7 +355,9 @@ def run_batch(a, rank, world, local, pg):
             "config": {"workload": BATCH_DESC, "boxes": len(boxes), "molecules": n, "precision": "mixed",
                        "autotune": tune, "parallelism": f"replicas x{world}",
                        "l2": "working set > L2 (state + lists of 2.7M molecules), no flush needed"},
-            "gpu_launches": 16 * a.steps,  # per step: pre, check, 11 rebuild kernels (early exit unless due), force, post, box sums
+            # per step: pre, check, force, post, box sums; 11 more in a step that rebuilds the list (a conditional
+            # node of the step graph)
+            "gpu_launches": 5 * a.steps + 11 * rebuilds_timed,
             "batch": {"rebuilds": rebuilds,
                       "errors_vs_fp64": "per box at the final state: Upot from the last step's record and the "
                                         "pressure (sum m v^2 + virial) / 3V against FP64 forces of the same positions",
@@ -486,20 +492,31 @@ def main():
     cu = Cudart()
 
     # ---- device-resident timing
+    rmm = a.integrator == "rmm"
+    mass = ps.components[0].lj[0].m if rmm else 1.0
+
+    def first_forces(e):
+        return e.rmm_forces(0.5 * dt / mass) if rmm else e.forces()
+
+    def steps(e, k, record):
+        return e.rmm_run(dt, k, record=record) if rmm else e.run(dt, k, record=record)
+
     eng = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local)
-    fo0 = eng.forces()
-    eng.run(dt, max(3, a.warmup), record=False)
+    fo0 = first_forces(eng)
+    steps(eng, max(3, a.warmup), False)
     eng.sync()
     stream = eng.stream()
     t_clock = ClockSampler(local)
     barrier(pg)
     e0, e1 = cu.event(), cu.event()
+    rb0 = eng.rebuilds()
     t_clock.start()
     cu.record(e0, stream)
-    eng.run(dt, a.steps, record=True)
+    steps(eng, a.steps, True)
     cu.record(e1, stream)
     ms = cu.elapsed_ms(e0, e1)
     clocks = t_clock.stop()
+    rebuilds_timed = eng.rebuilds() - rb0
     value, ms = replica_throughput(pg, world, n, a.steps, ms)
     # per-kernel times on the engine stream, right after the timed region
     fo = eng.forces()
@@ -524,9 +541,9 @@ def main():
         t0 = time.perf_counter()
         eng2 = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local)
         t_up = time.perf_counter()
-        eng2.forces()
+        first_forces(eng2)
         t_f = time.perf_counter()
-        rec = eng2.run(dt, a.steps, record=True)
+        rec = steps(eng2, a.steps, True)
         t_run = time.perf_counter()
         out = eng2.molecules()
         t1 = time.perf_counter()
@@ -552,8 +569,12 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-pairs/f64-state" if a.precision == "mixed" else "f64",
             "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann velocities)",
             "config": {"workload": desc, "precision": a.precision, "skin": skin, "molecules": n,
+                       "integrator": "LeapfrogRMM (reduced memory mode)" if rmm else "Leapfrog",
                        "parallelism": f"replicas x{world}", "l2": "working set > L2 (GBs), no flush needed"},
-            "gpu_launches": int(kt.launches_per_step * a.steps),
+            # graph-captured chunks of 25 steps: the per-step kernels, the rebuild kernels of the steps that
+            # rebuilt the list, and one pre-force half step per chunk where it is fused into the post-force one
+            "gpu_launches": int(kt.launches_per_step * a.steps + kt.launches_per_rebuild * rebuilds_timed
+                                + (0 if rmm else -(-a.steps // 25))),
             "roofline": {"bound": "hbm", "kernel": "k_force_lj32x2" if a.precision == "mixed" else "k_force_lj64",
                          "achieved": hbm_bytes / (kt.force_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                          "frac": hbm_bytes / (kt.force_ms * 1e-3) / 1e9 / hbm_peak,
@@ -566,7 +587,8 @@ def main():
                               "algorithmic": f"{FLOP_PER_PAIR_LJ:.0f} flop x {pairs} unique in-cutoff pairs per launch",
                               "peak_source": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 flop x 2070 MHz"},
             "kernels_ms": {"force": kt.force_ms, "pre": kt.pre_ms, "post": kt.post_ms, "rebuild": kt.rebuild_ms},
-            "pair_list": {"mean_candidates": kt.mean_candidates, "rebuilds": int(kt.rebuilds)},
+            "pair_list": {"mean_candidates": kt.mean_candidates, "rebuilds": int(kt.rebuilds),
+                          "rebuilds_timed": int(rebuilds_timed)},
             "physics": {"upot_per_molecule": fo.upot / n, "unique_lj_pairs": int(pairs)},
             "clocks": clocks,
             "e2e": e2e,

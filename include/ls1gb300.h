@@ -274,6 +274,28 @@ int md_thermostat_betas(md_ctx* ctx, int32_t thermostat, double* beta_trans, dou
 /* Wait for all work of the context. */
 int md_sync(md_ctx* ctx);
 
+/* ---- reduced memory mode (the reference's ENABLE_REDUCED_MEMORY_MODE build:
+ * MoleculeRMM, VCP1CLJRMM, LeapfrogRMM).  One component with a single LJ
+ * centre at the molecule centre (in mixed precision rc_lj = rc); forces are
+ * never stored.
+ * md_rmm_forces: VCP1CLJRMM traversal (VCP1CLJRMM.cpp:88-369): rebin and
+ *   rebuild when due, pair kernel that adds dt_inv_m * F to every velocity.
+ *   Simulation::prepare_start passes dt/(2m) for the initial force pass,
+ *   LeapfrogRMM steps dt/m (Simulation.cpp:902-938, VCP1CLJRMM.cpp:41-44).
+ *   Upot, virial and pair counts as md_compute_forces.  Replaces
+ *   VCP1CLJRMM::processCellPair/processCell/endTraversal.
+ * md_rmm_positions: r += dt v (LeapfrogRMM::computePositions,
+ *   PositionCellProcessorRMM.h:33-60).
+ * md_rmm_velocities: N and sum v.v, without the mass
+ *   (LeapfrogRMM::computeVelocities, VelocityCellProcessorRMM.h:95-128);
+ *   sumIw2 = 0, rot_dof = 0.
+ * md_rmm_run: nsteps LeapfrogRMM steps (positions, rebin when due, forces
+ *   with dt/m, velocity sums) as CUDA graphs; rec[k].summv2 = sum v.v. */
+int md_rmm_forces(md_ctx* ctx, double dt_inv_m, md_forces_out* out);
+int md_rmm_positions(md_ctx* ctx, double dt);
+int md_rmm_velocities(md_ctx* ctx, md_kinetic_out* out);
+int md_rmm_run(md_ctx* ctx, double dt, int32_t nsteps, md_step_record* rec);
+
 /* ---- measurement hooks (no counterpart in the reference; used by bench.py)
  * md_get_stream: the CUDA stream (cudaStream_t) every kernel of the context
  * runs on, so a caller can bracket calls with its own CUDA events.
@@ -287,13 +309,17 @@ typedef struct {
     double rebuild_ms;        /* one forced rebin + list rebuild                        */
     double mean_candidates;   /* mean pair-candidate list length per molecule           */
     int64_t rebuilds;         /* list rebuilds since md_create                          */
-    int32_t launches_per_step;/* kernels one md_run step launches                       */
-    int32_t reserved;
+    int32_t launches_per_step;/* kernels one graph-captured md_run step launches when
+                                 no list rebuild is due                                 */
+    int32_t launches_per_rebuild; /* kernels a list rebuild adds to such a step         */
     double adjoint_ms;        /* one md_adjoint kernel pass (gU = gW = 1, no gF),
                                  without its host copies                                */
 } md_kernel_times;
 
 int md_get_stream(md_ctx* ctx, void** stream);
+/* md_rebuilds: list rebuilds since md_create (device counter, read after the
+ * stream's work so far). */
+int md_rebuilds(md_ctx* ctx, int64_t* count);
 int md_time_kernels(md_ctx* ctx, int32_t reps, md_kernel_times* out);
 
 /* ---- batches of independent boxes (no counterpart in the reference, which

@@ -200,22 +200,27 @@ __global__ void k_finalize1(const double* partials, int pstride, int nw_force, i
     if (threadIdx.x == 0) seg[s * FIN_SEG + b] = v;
 }
 
-__global__ void k_finalize2(const double* seg, double* result) {
+// Second stage of the fixed-order sums (one warp, one slot per lane); with
+// rec, also the step record (Upot, virial, sum m v^2, sum I w^2) of the
+// step counted by *step.
+__global__ void k_finalize2(const double* seg, double* result, md_step_record* rec, int* step, int has_rot_dof) {
     const int s = threadIdx.x;
-    if (s >= NPART) return;
     double v = 0.0;
-    for (int b = 0; b < FIN_SEG; ++b) v += seg[s * FIN_SEG + b];
-    result[s] = v;
-}
-
-__global__ void k_record(const double* result, md_step_record* rec, int* step, int has_rot_dof) {
-    int k = *step;
-    double myRF = result[3];
-    rec[k].upot = result[0] / 6.0 + result[1] + myRF;
-    rec[k].virial = result[2] + 3.0 * myRF;
-    rec[k].summv2 = result[12];
-    rec[k].sumIw2 = has_rot_dof ? result[13] : 0.0;
-    *step = k + 1;
+    if (s < NPART)
+        for (int b = 0; b < FIN_SEG; ++b) v += seg[s * FIN_SEG + b];
+    if (s < NPART) result[s] = v;
+    if (!rec) return;  // uniform over the warp
+    const double u6 = __shfl_sync(0xffffffffu, v, 0), ux = __shfl_sync(0xffffffffu, v, 1);
+    const double vir = __shfl_sync(0xffffffffu, v, 2), myRF = __shfl_sync(0xffffffffu, v, 3);
+    const double mv2 = __shfl_sync(0xffffffffu, v, 12), iw2 = __shfl_sync(0xffffffffu, v, 13);
+    if (s == 0) {
+        const int k = *step;
+        rec[k].upot = u6 / 6.0 + ux + myRF;
+        rec[k].virial = vir + 3.0 * myRF;
+        rec[k].summv2 = mv2;
+        rec[k].sumIw2 = has_rot_dof ? iw2 : 0.0;
+        *step = k + 1;
+    }
 }
 
 // ------------------------------------------------------------------ wrap + cells
@@ -964,13 +969,26 @@ __device__ __forceinline__ void lj_pack2(const float2 pix, const float2 piy, con
 // frame), so Upot, virial and the pair count are half the per-molecule
 // sums over all neighbours.  Force sums are Kahan-compensated per group of
 // four candidates; eps24 multiplies the sums once per molecule.
+//
+// Epilogues: EPI_STORE writes F, M (zero) and Vi into the state.  EPI_RMM is
+// the reduced memory mode's cell processor (VCP1CLJRMM.cpp:240-369): no force
+// is stored, the kick v += dt_inv_m F is applied at once (dt_inv_m = dt / m,
+// halved for the initial force pass), and with sum_v2 the kernel also
+// contributes sum v.v of the kicked velocities (VelocityCellProcessorRMM.h:
+// 95-128, no mass) to slot 12.
+#define EPI_STORE 0
+#define EPI_RMM 1
+// v.v of the reduced mode's velocity sums (one expression for every kernel
+// that forms it, so their per-warp partials agree bit for bit)
+__device__ __forceinline__ double rmm_v2(double x, double y, double z) { return x * x + y * y + z * z; }
 #ifndef MD_LJX2_MIN_BLOCKS
 #define MD_LJX2_MIN_BLOCKS 3  // blocks of 256 per SM the register budget is sized for
 #endif
+template <int EPI>
 __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State S, const float4* __restrict__ xlf,
                                                          const uint32_t* __restrict__ nbr,
                                                          const int* __restrict__ nnb, int maxnb, double* partials,
-                                                         int pstride) {
+                                                         int pstride, double dt_inv_m, int sum_v2) {
     // minus the offset of the neighbour cell's origin (code) from the home cell's origin, one table per
     // axis: three conflict-free 4-byte shared loads per candidate move fewer shared-memory wavefronts
     // than one 16-byte load (which also conflicts between codes 8 apart)
@@ -984,6 +1002,7 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float up = 0.f, vir = 0.f, npairs = 0.f;  // halved per-molecule sums (every pair is seen twice)
+    float v2f = 0.f;                          // EPI_RMM: v.v after the kick
     if (i < S.n) {
         const float4 p4 = xlf[i];
         const int gi = cP.comp[__float_as_int(p4.w)].ljoff;
@@ -1033,11 +1052,20 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
         // epilogue in FP32 (the precision of the pair sums) with exact conversions to the FP64 state
         const float nin = a.nin.x + a.nin.y;
         const float vx = e24 * (a.vx.x + a.vx.y), vy = e24 * (a.vy.x + a.vy.y), vz = e24 * (a.vz.x + a.vz.y);
-        S.Fx[i] = f2d_exact(e24 * (fx.s - fx.c));
-        S.Fy[i] = f2d_exact(e24 * (fy.s - fy.c));
-        S.Fz[i] = f2d_exact(e24 * (fz.s - fz.c));
-        S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
-        S.Vx[i] = f2d_exact(0.5f * vx); S.Vy[i] = f2d_exact(0.5f * vy); S.Vz[i] = f2d_exact(0.5f * vz);
+        if (EPI == EPI_STORE) {
+            S.Fx[i] = f2d_exact(e24 * (fx.s - fx.c));
+            S.Fy[i] = f2d_exact(e24 * (fy.s - fy.c));
+            S.Fz[i] = f2d_exact(e24 * (fz.s - fz.c));
+            S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
+            S.Vx[i] = f2d_exact(0.5f * vx); S.Vy[i] = f2d_exact(0.5f * vy); S.Vz[i] = f2d_exact(0.5f * vz);
+        } else {
+            const double ux = S.vx[i] + dt_inv_m * f2d_exact(e24 * (fx.s - fx.c));
+            const double uy = S.vy[i] + dt_inv_m * f2d_exact(e24 * (fy.s - fy.c));
+            const double uz = S.vz[i] + dt_inv_m * f2d_exact(e24 * (fz.s - fz.c));
+            S.vx[i] = ux; S.vy[i] = uy; S.vz[i] = uz;
+            const float gx = d2f_int(ux), gy = d2f_int(uy), gz = d2f_int(uz);
+            v2f = gx * gx + (gy * gy + gz * gz);
+        }
         up = 0.5f * (e24 * (a.up.x + a.up.y) + sh6 * nin);
         vir = 0.5f * (vx + (vy + vz));
         npairs = 0.5f * nin;
@@ -1049,15 +1077,20 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
     warp_partial_count(partials, pstride, 4, npairs);
     warp_partial_count(partials, pstride, 5, npairs);
     for (int sl = 6; sl < 12; ++sl) warp_partial_zero(partials, pstride, sl);
+    if (EPI == EPI_RMM && sum_v2) warp_partial_f32(partials, pstride, 12, v2f);
 }
 
 // FP64 variant: absolute FP64 positions with the reference's halo image
-// shift r_j +- L, FP64 arithmetic and accumulation throughout.
+// shift r_j +- L, FP64 arithmetic and accumulation throughout; epilogues as
+// in k_force_lj32x2.
+template <int EPI>
 __global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __restrict__ xlf,
                                                     const uint32_t* __restrict__ nbr, const int* __restrict__ nnb,
-                                                    int maxnb, double* partials, int pstride) {
+                                                    int maxnb, double* partials, int pstride, double dt_inv_m,
+                                                    int sum_v2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double fx = 0, fy = 0, fz = 0, vx = 0, vy = 0, vz = 0, up = 0, vir = 0;
+    double v2 = 0.0;  // EPI_RMM: v.v after the kick
     int npairs = 0, nmol = 0;
     if (i < S.n) {
         const int ci = S.comp[i];
@@ -1092,9 +1125,15 @@ __global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __res
                 ++npairs;
             }
         }
-        S.Fx[i] = fx; S.Fy[i] = fy; S.Fz[i] = fz;
-        S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
-        S.Vx[i] = 0.5 * vx; S.Vy[i] = 0.5 * vy; S.Vz[i] = 0.5 * vz;
+        if (EPI == EPI_STORE) {
+            S.Fx[i] = fx; S.Fy[i] = fy; S.Fz[i] = fz;
+            S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
+            S.Vx[i] = 0.5 * vx; S.Vy[i] = 0.5 * vy; S.Vz[i] = 0.5 * vz;
+        } else {
+            const double ux = S.vx[i] + dt_inv_m * fx, uy = S.vy[i] + dt_inv_m * fy, uz = S.vz[i] + dt_inv_m * fz;
+            S.vx[i] = ux; S.vy[i] = uy; S.vz[i] = uz;
+            v2 = rmm_v2(ux, uy, uz);
+        }
     }
     warp_partial(partials, pstride, 0, up);
     warp_partial_zero(partials, pstride, 1);
@@ -1103,6 +1142,7 @@ __global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __res
     warp_partial_count(partials, pstride, 4, (float)nmol);
     warp_partial_count(partials, pstride, 5, (float)npairs);
     for (int sl = 6; sl < 12; ++sl) warp_partial_zero(partials, pstride, sl);
+    if (EPI == EPI_RMM && sum_v2) warp_partial(partials, pstride, 12, v2);
 }
 
 // ---------------------------------------------------------------- multi-site
@@ -1485,15 +1525,61 @@ __global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const 
     }
 }
 
+// Reduced memory mode, PositionCellProcessorRMM::processCell
+// (PositionCellProcessorRMM.h:33-60): r += dt v for every molecule, nothing
+// else; then the FP32 local coordinates and the displacement since the last
+// list build, as in k_pre.
+__global__ void k_rmm_drift(State S, double dt, float4* xlf, const double* origin, const float4* xlref,
+                            unsigned* disp_max) {
+    __shared__ float smax[8];
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float d2 = 0.f;
+    if (i < S.n) {
+        const double rx = S.rx[i] + dt * S.vx[i], ry = S.ry[i] + dt * S.vy[i], rz = S.rz[i] + dt * S.vz[i];
+        S.rx[i] = rx; S.ry[i] = ry; S.rz[i] = rz;
+        const float4 q0 = xlref[i];
+        float4 p;
+        p.x = d2f_int(rx - origin[3 * i]);
+        p.y = d2f_int(ry - origin[3 * i + 1]);
+        p.z = d2f_int(rz - origin[3 * i + 2]);
+        p.w = q0.w;
+        xlf[i] = p;
+        const float ddx = p.x - q0.x, ddy = p.y - q0.y, ddz = p.z - q0.z;
+        d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+    }
+    for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, o));
+    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = d2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, smax[w]);
+        atomicMax(disp_max, __float_as_uint(m));
+    }
+}
+
+// VelocityCellProcessorRMM::processCell (VelocityCellProcessorRMM.h:95-128):
+// sum v.v over all molecules (no mass) into slot 12.
+__global__ void k_rmm_vsum(State S, double* partials, int pstride) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double v2 = 0.0;
+    if (i < S.n) v2 = rmm_v2(S.vx[i], S.vy[i], S.vz[i]);
+    warp_partial(partials, pstride, 12, v2);
+}
+
 // Rebuild when two molecules may have approached by more than the skin.
+// Inside a captured graph the decision also sets the condition of the IF
+// node that holds the rebuild kernels (cond != 0), so a step without a
+// rebuild launches none of them.
 __global__ void k_check_rebuild(unsigned* disp_max, unsigned* need, float half_skin2, int force,
-                                unsigned long long* nrebuild) {
+                                unsigned long long* nrebuild, cudaGraphConditionalHandle cond) {
     float m = __uint_as_float(*disp_max);
-    *need = (force || m > half_skin2) ? 1u : 0u;
-    if (*need) {
+    const unsigned go = (force || m > half_skin2) ? 1u : 0u;
+    *need = go;
+    if (go) {
         *disp_max = 0u;
         *nrebuild += 1ull;
     }
+    if (cond) cudaGraphSetConditional(cond, go);
 }
 
 __global__ void k_sum_int(const int* a, int64_t n, unsigned long long* out) {

@@ -58,10 +58,15 @@ def load_library(path: str = LIB_PATH):
     L.md_integrate_pre.argtypes = [vp, d]
     L.md_integrate_post.argtypes = [vp, d, C.POINTER(abi.MdKineticOut)]
     L.md_run.argtypes = [vp, d, i32, C.POINTER(abi.MdStepRecord)]
+    L.md_rmm_forces.argtypes = [vp, d, C.POINTER(abi.MdForcesOut)]
+    L.md_rmm_positions.argtypes = [vp, d]
+    L.md_rmm_velocities.argtypes = [vp, C.POINTER(abi.MdKineticOut)]
+    L.md_rmm_run.argtypes = [vp, d, i32, C.POINTER(abi.MdStepRecord)]
     L.md_sync.argtypes = [vp]
     L.md_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.md_adjoint.argtypes = [vp, d, d, vp, vp, vp, i32]
     L.md_time_kernels.argtypes = [vp, i32, C.POINTER(abi.MdKernelTimes)]
+    L.md_rebuilds.argtypes = [vp, C.POINTER(i64)]
     L.md_longrange_homogeneous.argtypes = [vp, i32, dp, dp]
     L.md_set_thermostat.argtypes = [vp, d, i32]
     L.md_apply_thermostat.argtypes = [vp, dp, dp]
@@ -155,6 +160,29 @@ class Engine:
             return None
         return np.array([[x.upot, x.virial, x.summv2, x.sumIw2] for x in rec[:nsteps]])
 
+    # ---- reduced memory mode (LeapfrogRMM + VCP1CLJRMM)
+    def rmm_forces(self, dt_inv_m: float) -> abi.MdForcesOut:
+        """Force pass that adds dt_inv_m * F to every velocity (no force stored)."""
+        out = abi.MdForcesOut()
+        self._check(self.L.md_rmm_forces(self.h, dt_inv_m, C.byref(out)), "md_rmm_forces")
+        return out
+
+    def rmm_positions(self, dt: float):
+        self._check(self.L.md_rmm_positions(self.h, dt), "md_rmm_positions")
+
+    def rmm_velocities(self) -> abi.MdKineticOut:
+        out = abi.MdKineticOut()
+        self._check(self.L.md_rmm_velocities(self.h, C.byref(out)), "md_rmm_velocities")
+        return out
+
+    def rmm_run(self, dt: float, nsteps: int, record: bool = True) -> Optional[np.ndarray]:
+        """nsteps LeapfrogRMM steps; rows (Upot, virial, sum v.v, 0)."""
+        rec = (abi.MdStepRecord * max(nsteps, 1))() if record else None
+        self._check(self.L.md_rmm_run(self.h, dt, nsteps, rec), "md_rmm_run")
+        if not record:
+            return None
+        return np.array([[x.upot, x.virial, x.summv2, x.sumIw2] for x in rec[:nsteps]])
+
     def sync(self):
         self._check(self.L.md_sync(self.h), "md_sync")
 
@@ -163,6 +191,12 @@ class Engine:
         s = C.c_void_p()
         self._check(self.L.md_get_stream(self.h, C.byref(s)), "md_get_stream")
         return s.value or 0
+
+    def rebuilds(self) -> int:
+        """List rebuilds since the context was created."""
+        c = C.c_int64()
+        self._check(self.L.md_rebuilds(self.h, C.byref(c)), "md_rebuilds")
+        return c.value
 
     def time_kernels(self, reps: int = 10) -> abi.MdKernelTimes:
         t = abi.MdKernelTimes()
@@ -306,3 +340,27 @@ class GpuLeapfrog:
 
     def eventForcesCalculated(self, cells: GpuLinkedCells) -> abi.MdKineticOut:
         return cells.engine.post(self.dt)
+
+
+class GpuLeapfrogRMM:
+    """Mirror of LeapfrogRMM with its cell processors (LeapfrogRMM.cpp:42-107,
+    VCP1CLJRMM.cpp:41-44, Simulation.cpp:902-938): prepare() is the initial
+    force pass with the half kick dt/(2m), then per step eventNewTimestep
+    (positions), traverseCells (forces with the kick dt/m) and
+    eventForcesCalculated (N, sum v.v)."""
+
+    def __init__(self, dt: float, mass: float):
+        self.dt = dt
+        self.dt_inv_m = dt / mass
+
+    def prepare(self, cells: GpuLinkedCells) -> abi.MdForcesOut:
+        return cells.engine.rmm_forces(self.dt_inv_m * 0.5)
+
+    def eventNewTimestep(self, cells: GpuLinkedCells):
+        cells.engine.rmm_positions(self.dt)
+
+    def traverseCells(self, cells: GpuLinkedCells) -> abi.MdForcesOut:
+        return cells.engine.rmm_forces(self.dt_inv_m)
+
+    def eventForcesCalculated(self, cells: GpuLinkedCells) -> abi.MdKineticOut:
+        return cells.engine.rmm_velocities()

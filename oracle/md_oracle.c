@@ -1177,6 +1177,66 @@ int orc_run(orc_sys* s, double dt, int32_t nsteps, md_step_record* rec) {
     return MD_OK;
 }
 
+/* ---------------------------------------------------------------- reduced memory mode
+ * VCP1CLJRMM (VCP1CLJRMM.cpp:240-369) computes the single-centre LJ pairs of
+ * the same traversal and adds dt_inv_m times each pair force to the two
+ * velocities at once instead of storing forces; here the traversal's forces
+ * are summed first and added once per molecule (the same sum in another
+ * order).  Upot = upot6lj / 6 and the virial as in VCP::endTraversal. */
+int orc_rmm_forces(orc_sys* s, double dt_inv_m, md_forces_out* out) {
+    int rc = orc_rebin_and_halo(s, NULL);
+    if (rc) return rc;
+    orc_forces(s, out, NULL);
+    for (int64_t k = 0; k < 3 * s->n; ++k) s->v[k] += dt_inv_m * s->F[k];
+    return MD_OK;
+}
+
+/* PositionCellProcessorRMM::processCell (PositionCellProcessorRMM.h:33-60) */
+int orc_rmm_positions(orc_sys* s, double dt) {
+    for (int64_t k = 0; k < 3 * s->n; ++k) s->r[k] += dt * s->v[k];
+    return MD_OK;
+}
+
+/* VelocityCellProcessorRMM::processCell (VelocityCellProcessorRMM.h:95-128):
+ * sum of v.v, no mass; LeapfrogRMM::computeVelocities reports it with
+ * sumIw2 = 0 and no rotational degrees of freedom (LeapfrogRMM.cpp:97-105). */
+int orc_rmm_velocities(const orc_sys* s, md_kinetic_out* out) {
+    double sum = 0.0;
+    for (int64_t k = 0; k < s->n; ++k) {
+        const double* v = s->v + 3 * k;
+        sum += v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    }
+    if (out) {
+        out->summv2 = sum;
+        out->sumIw2 = 0.0;
+        out->n = s->n;
+        out->rot_dof = 0;
+    }
+    return MD_OK;
+}
+
+/* One LeapfrogRMM step per iteration: eventNewTimestep (positions), the
+ * container update, the force traversal with dt_inv_m = dt / m
+ * (VCP1CLJRMM.cpp:41-44), eventForcesCalculated (velocity sums). */
+int orc_rmm_run(orc_sys* s, double dt, int32_t nsteps, md_step_record* rec) {
+    const double dt_inv_m = dt / s->cdef[0].m;
+    for (int32_t k = 0; k < nsteps; ++k) {
+        orc_rmm_positions(s, dt);
+        md_forces_out fo;
+        int rc = orc_rmm_forces(s, dt_inv_m, &fo);
+        if (rc) return rc;
+        md_kinetic_out ko;
+        orc_rmm_velocities(s, &ko);
+        if (rec) {
+            rec[k].upot = fo.upot;
+            rec[k].virial = fo.virial;
+            rec[k].summv2 = ko.summv2;
+            rec[k].sumIw2 = 0.0;
+        }
+    }
+    return MD_OK;
+}
+
 /* ---------------------------------------------------------------- long range
  * Homogeneous::init + calculateLongRange (src/longRange/Homogeneous.cpp:22-146)
  * with its tail integrals (Homogeneous.cpp:158-196): for every pair of LJ

@@ -40,6 +40,13 @@ int orc_forces(orc_sys* s, md_forces_out* out, double* kernel_calls);
 int orc_pre(orc_sys* s, double dt);
 int orc_post(orc_sys* s, double dt, md_kinetic_out* out);
 int orc_run(orc_sys* s, double dt, int32_t nsteps, md_step_record* rec);
+/* reduced memory mode (LeapfrogRMM + VCP1CLJRMM): forces with the velocity
+ * kick v += dt_inv_m F, drift r += dt v, velocity sums v.v without the mass,
+ * and whole steps */
+int orc_rmm_forces(orc_sys* s, double dt_inv_m, md_forces_out* out);
+int orc_rmm_positions(orc_sys* s, double dt);
+int orc_rmm_velocities(const orc_sys* s, md_kinetic_out* out);
+int orc_rmm_run(orc_sys* s, double dt, int32_t nsteps, md_step_record* rec);
 /* global velocity-scaling thermostat (target <= 0: NVE), applied by orc_run */
 int orc_set_thermostat(orc_sys* s, double target_temperature, int32_t explosion_heuristics);
 int orc_thermostat(orc_sys* s, const md_kinetic_out* ko, double* beta_trans, double* beta_rot);

@@ -50,6 +50,10 @@ def lib():
         L.orc_pre.argtypes = [vp, C.c_double]
         L.orc_post.argtypes = [vp, C.c_double, C.POINTER(abi.MdKineticOut)]
         L.orc_run.argtypes = [vp, C.c_double, i32, C.POINTER(abi.MdStepRecord)]
+        L.orc_rmm_forces.argtypes = [vp, C.c_double, C.POINTER(abi.MdForcesOut)]
+        L.orc_rmm_positions.argtypes = [vp, C.c_double]
+        L.orc_rmm_velocities.argtypes = [vp, C.POINTER(abi.MdKineticOut)]
+        L.orc_rmm_run.argtypes = [vp, C.c_double, i32, C.POINTER(abi.MdStepRecord)]
         L.orc_longrange_homogeneous.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_set_thermostat.argtypes = [vp, C.c_double, i32]
         _lib = L
@@ -125,6 +129,29 @@ class Oracle:
         rc = lib().orc_run(self.h, dt, nsteps, rec)
         if rc:
             raise RuntimeError(f"orc_run: {rc}")
+        return np.array([[x.upot, x.virial, x.summv2, x.sumIw2] for x in rec[:nsteps]])
+
+    def rmm_forces(self, dt_inv_m):
+        """Reduced memory mode force pass: forces, then v += dt_inv_m F."""
+        fo = abi.MdForcesOut()
+        rc = lib().orc_rmm_forces(self.h, dt_inv_m, C.byref(fo))
+        if rc:
+            raise RuntimeError(f"orc_rmm_forces: {rc}")
+        return fo
+
+    def rmm_positions(self, dt):
+        lib().orc_rmm_positions(self.h, dt)
+
+    def rmm_velocities(self):
+        ko = abi.MdKineticOut()
+        lib().orc_rmm_velocities(self.h, C.byref(ko))
+        return ko
+
+    def rmm_run(self, dt, nsteps):
+        rec = (abi.MdStepRecord * max(nsteps, 1))()
+        rc = lib().orc_rmm_run(self.h, dt, nsteps, rec)
+        if rc:
+            raise RuntimeError(f"orc_rmm_run: {rc}")
         return np.array([[x.upot, x.virial, x.summv2, x.sumIw2] for x in rec[:nsteps]])
 
     def molecules(self):
