@@ -540,6 +540,29 @@ __global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, con
     xlref[i] = p;
 }
 
+// Pair-candidate rows of the thread-per-molecule kernels (single-centre LJ)
+// are interleaved in 32-byte blocks (one DRAM sector) across the 32
+// molecules of a warp: block c (entries 8c .. 8c + 7) of molecule i is block
+// ((i / 32) * (maxnb / 8) + c) * 32 + i % 32 of the list, so the lanes of a
+// warp read one kilobyte of consecutive bytes per block instead of one
+// sector from each of 32 rows, and the list build writes whole sectors.
+// The rows of the warp-per-molecule kernels (multi-site) stay row-major
+// (row i at i * maxnb).  maxnb is a multiple of 8.
+__device__ __forceinline__ size_t il_block(int64_t i, int c, int maxnb) {
+    return ((size_t)(i >> 5) * (size_t)(maxnb >> 3) + (size_t)c) * 32 + (size_t)(i & 31);
+}
+__device__ __forceinline__ size_t il_entry(int64_t i, int k, int maxnb) {
+    return il_block(i, k >> 3, maxnb) * 8 + (size_t)(k & 7);
+}
+// 16-byte chunk q (entries 4q .. 4q + 3) of an interleaved row, relative to
+// the row's first chunk
+__device__ __forceinline__ int il_q(int q) { return (q >> 1) * 64 + (q & 1); }
+// Entry k of a row relative to the row's entry 0 (interleaved or row-major).
+template <bool IL>
+__device__ __forceinline__ int row_off(int k) {
+    return IL ? (k >> 3) * 256 + (k & 7) : k;
+}
+
 #define BL_WARPS 4
 #define BL_BUF 8
 // Geometry of one box's list grid: cells per axis, cell edges, periodicity,
@@ -558,6 +581,7 @@ struct ListGrid {
 // shifted coordinates (unused slots far away); every lane tests its molecule
 // against them, two per paired FP32 instruction, into a hit mask, then
 // appends the hits in candidate order.
+template <bool IL>
 __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, const int* start, const ListGrid& g,
                                                 int lc, uint32_t* nbr, int* nnb, int maxnb, float rl2,
                                                 unsigned* status, int* need_max, float* sq,
@@ -576,7 +600,8 @@ __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, con
         if (own) pi = xl[i];
         const float2 pix = make_float2(pi.x, pi.x), piy = make_float2(pi.y, pi.y), piz = make_float2(pi.z, pi.z);
         int cnt = 0, nb = 0;
-        uint32_t* row = nbr + (size_t)(own ? i : 0) * maxnb;
+        const int64_t il = own ? i : 0;
+        uint32_t* row = IL ? nbr + il_block(il, 0, maxnb) * 8 : nbr + (size_t)il * maxnb;
         for (int oz = -1; oz <= 1; ++oz)
             for (int oy = -1; oy <= 1; ++oy)
                 for (int ox = -1; ox <= 1; ++ox) {
@@ -631,11 +656,11 @@ __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, con
                             buf[nb++] = e0 + (uint32_t)t;
                             if (nb == BL_BUF) {
                                 if (cnt + BL_BUF <= maxnb) {
-                                    uint4* dst = reinterpret_cast<uint4*>(row + cnt);
+                                    uint4* dst = reinterpret_cast<uint4*>(row + row_off<IL>(cnt));
                                     dst[0] = make_uint4(buf[0], buf[1], buf[2], buf[3]);
                                     dst[1] = make_uint4(buf[4], buf[5], buf[6], buf[7]);
                                 } else {
-                                    for (int u = 0; u < BL_BUF && cnt + u < maxnb; ++u) row[cnt + u] = buf[u];
+                                    for (int u = 0; u < BL_BUF && cnt + u < maxnb; ++u) row[row_off<IL>(cnt + u)] = buf[u];
                                 }
                                 cnt += BL_BUF;
                                 nb = 0;
@@ -644,11 +669,11 @@ __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, con
                     }
                 }
         if (own) {
-            for (int u = 0; u < nb && cnt + u < maxnb; ++u) row[cnt + u] = buf[u];
+            for (int u = 0; u < nb && cnt + u < maxnb; ++u) row[row_off<IL>(cnt + u)] = buf[u];
             cnt += nb;
             // pad the row to a multiple of four with the far-away slot n (zero cell offset)
             const uint32_t pad = (uint32_t)n | (13u << MD_CODE_SHIFT);
-            for (int u = cnt; u < ((cnt + 3) & ~3) && u < maxnb; ++u) row[u] = pad;
+            for (int u = cnt; u < ((cnt + 3) & ~3) && u < maxnb; ++u) row[row_off<IL>(u)] = pad;
             nnb[i] = min(cnt, maxnb);
             if (cnt > maxnb) {
                 atomicOr(status, ST_LIST_OVERFLOW);
@@ -665,11 +690,13 @@ __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, con
 // (coalesced load, already shifted into the home cell's frame); every lane
 // tests its molecule against the staged candidates (broadcast reads, two
 // per paired FP32 instruction) and appends hits to its own 8-entry
-// shared-memory buffer, flushed as two 16-byte stores into its row.  Rows
-// are row-major (row i at i * maxnb, maxnb a multiple of 4).  Candidate test in FP32 local coordinates against
+// shared-memory buffer, flushed as one 32-byte block into its row (IL:
+// interleaved rows for the thread-per-molecule kernels, else row-major).
+// Candidate test in FP32 local coordinates against
 // (rc + skin)^2 enlarged by a relative 2e-4, so no pair that can come within
 // rc before the next rebuild is missed.
-__global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const float4* xl, const int* start,
+template <bool IL>
+__global__ void __launch_bounds__(BL_WARPS * 32, 8) k_build_list(int64_t n, const float4* xl, const int* start,
                                                               int ncells, uint32_t* nbr, int* nnb, int maxnb,
                                                               float rl2, unsigned* status, int* need_max,
                                                               const unsigned* need) {
@@ -686,7 +713,7 @@ __global__ void __launch_bounds__(BL_WARPS * 32) k_build_list(int64_t n, const f
         g.per[d] = cP.periodic[d] != 0;
     }
     g.base = 0;
-    build_cell_rows(n, xl, start, g, c, nbr, nnb, maxnb, rl2, status, need_max, &sq[wl][0][0], sbuf[wl], lane);
+    build_cell_rows<IL>(n, xl, start, g, c, nbr, nnb, maxnb, rl2, status, need_max, &sq[wl][0][0], sbuf[wl], lane);
 }
 
 // ------------------------------------------------------------------ site cache
@@ -769,9 +796,9 @@ __global__ void __launch_bounds__(256, 4) k_force_lj32(State S, const float4* __
         float e24 = cP.eps24f[gi * cP.nlj + gi], s2 = cP.sig2f[gi * cP.nlj + gi];
         float sh6 = cP.shift6f[gi * cP.nlj + gi];
         int cur = gi;
-        const uint4* row = reinterpret_cast<const uint4*>(nbr + (size_t)i * maxnb);
+        const uint4* row = reinterpret_cast<const uint4*>(nbr + il_block(i, 0, maxnb) * 8);
         for (int k = 0; k < cnt; k += 4) {
-            const uint4 e4 = __ldg(row + (k >> 2));
+            const uint4 e4 = __ldg(row + il_q(k >> 2));
             const uint32_t ee[4] = {e4.x, e4.y, e4.z, e4.w};
             float4 pj[4];
 #pragma unroll
@@ -1018,11 +1045,11 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
         a.vx = a.vy = a.vz = a.up = a.nin = make_float2(0.f, 0.f);
         AmbList am;
         am.n = 0;
-        const uint4* row = reinterpret_cast<const uint4*>(nbr + (size_t)i * maxnb);
+        const uint4* row = reinterpret_cast<const uint4*>(nbr + il_block(i, 0, maxnb) * 8);
         uint4 nx = cnt > 0 ? ld_row_chunk(row) : make_uint4(0u, 0u, 0u, 0u);
         for (int k = 0; k < cnt; k += 4) {
             const uint4 e4 = nx;
-            if (k + 4 < cnt) nx = ld_row_chunk(row + (k >> 2) + 1);
+            if (k + 4 < cnt) nx = ld_row_chunk(row + il_q((k >> 2) + 1));
             const float4 pa = __ldg(&xlf[e4.x & MD_INDEX_MASK]), pb = __ldg(&xlf[e4.y & MD_INDEX_MASK]);
             const float4 pc = __ldg(&xlf[e4.z & MD_INDEX_MASK]), pd = __ldg(&xlf[e4.w & MD_INDEX_MASK]);
             a.gx = a.gy = a.gz = make_float2(0.f, 0.f);
@@ -1040,7 +1067,7 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
             const bool listed = am.n <= MD_AMB;
             const int m = listed ? am.n : cnt;
             for (int t = 0; t < m; ++t) {
-                const uint32_t en = listed ? am.e[t] : nbr[(size_t)i * maxnb + t];
+                const uint32_t en = listed ? am.e[t] : nbr[il_entry(i, t, maxnb)];
                 const int j = (int)(en & MD_INDEX_MASK);
                 const uint32_t code = en >> MD_CODE_SHIFT;
                 float dx, dy, dz;
@@ -1098,9 +1125,8 @@ __global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __res
         const double pix = S.rx[i], piy = S.ry[i], piz = S.rz[i];
         const int h = S.home[i];
         const int cnt = nnb[i];
-        const uint32_t* row = nbr + (size_t)i * maxnb;
         for (int k = 0; k < cnt; ++k) {
-            const uint32_t e = __ldg(row + k);
+            const uint32_t e = __ldg(nbr + il_entry(i, k, maxnb));
             const int j = (int)(e & MD_INDEX_MASK);
             const uint32_t code = e >> MD_CODE_SHIFT;
             double shf[3];
