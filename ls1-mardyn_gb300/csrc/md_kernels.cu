@@ -575,12 +575,59 @@ struct ListGrid {
     int base;
 };
 
+// Tests this lane's molecule against the m staged candidates (negated,
+// shifted coordinates sx/sy/sz, list entries se; slots m .. 31 far away when
+// m < 32), two per paired FP32 instruction, and appends the hits to the
+// lane's shared-memory buffer, flushing it to the row in 32-byte blocks.
+template <bool IL>
+__device__ __forceinline__ void test_staged(int m, const float2 pix, const float2 piy, const float2 piz, float rl2,
+                                            const float* sx, const float* sy, const float* sz, const uint32_t* se,
+                                            bool own, uint32_t self, uint32_t* buf, int& nb, int& cnt, uint32_t* row,
+                                            int maxnb) {
+    uint32_t hits = 0u;
+    const int mm = (m + 1) & ~1;  // pairs of staged slots; slot m (if odd) is far away
+#pragma unroll 4
+    for (int t = 0; t < mm; t += 2) {
+        const float2 dx = __fadd2_rn(pix, *reinterpret_cast<const float2*>(sx + t));
+        const float2 dy = __fadd2_rn(piy, *reinterpret_cast<const float2*>(sy + t));
+        const float2 dz = __fadd2_rn(piz, *reinterpret_cast<const float2*>(sz + t));
+        float2 r2 = __fmul2_rn(dz, dz);
+        r2 = __ffma2_rn(dy, dy, r2);
+        r2 = __ffma2_rn(dx, dx, r2);
+        hits |= (r2.x < rl2 ? 1u : 0u) << t;
+        hits |= (r2.y < rl2 ? 1u : 0u) << (t + 1);
+    }
+    if (!own) hits = 0u;
+    while (hits) {
+        const int t = __ffs(hits) - 1;
+        hits &= hits - 1u;
+        const uint32_t en = se[t];
+        if (en == self) continue;  // not the molecule itself
+        buf[nb++] = en;
+        if (nb == BL_BUF) {
+            if (cnt + BL_BUF <= maxnb) {
+                uint4* dst = reinterpret_cast<uint4*>(row + row_off<IL>(cnt));
+                dst[0] = make_uint4(buf[0], buf[1], buf[2], buf[3]);
+                dst[1] = make_uint4(buf[4], buf[5], buf[6], buf[7]);
+            } else {
+                for (int u = 0; u < BL_BUF && cnt + u < maxnb; ++u) row[row_off<IL>(cnt + u)] = buf[u];
+            }
+            cnt += BL_BUF;
+            nb = 0;
+        }
+    }
+}
+
 // Rows of the molecules of list cell `lc` (local index in grid g), built by
-// one warp; sq (3 x 32 floats) and sbuf are this warp's shared-memory areas.
-// Each batch of up to 32 candidates of a neighbour cell is staged as negated,
-// shifted coordinates (unused slots far away); every lane tests its molecule
-// against them, two per paired FP32 instruction, into a hit mask, then
-// appends the hits in candidate order.
+// one warp; sq (4 x 32 words) and sbuf are this warp's shared-memory areas.
+// For up to 32 home molecules at a time (one per lane) the warp streams the
+// candidates of the 27 neighbour cells in order; a candidate farther from
+// the bounding box of the home molecules than the list radius (enlarged by
+// a relative 1e-4, so FP32 rounding cannot drop a pair the exact test
+// keeps) is skipped, the others are compacted into a staging area of 32
+// (negated coordinates shifted into the home cell's frame, and their list
+// entries), and every full staging area is tested by all lanes at once.
+// The rows keep the candidates in neighbour-cell and slot order.
 template <bool IL>
 __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, const int* start, const ListGrid& g,
                                                 int lc, uint32_t* nbr, int* nnb, int maxnb, float rl2,
@@ -593,13 +640,27 @@ __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, con
     float* sx = sq;
     float* sy = sq + 32;
     float* sz = sq + 64;
+    uint32_t* se = reinterpret_cast<uint32_t*>(sq + 96);
+    const float pre2 = rl2 * 1.0001f;
     for (int i0 = b; i0 < e; i0 += 32) {
         const int i = i0 + lane;
         const bool own = i < e;
         float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
         if (own) pi = xl[i];
         const float2 pix = make_float2(pi.x, pi.x), piy = make_float2(pi.y, pi.y), piz = make_float2(pi.z, pi.z);
-        int cnt = 0, nb = 0;
+        // bounding box of this group of home molecules
+        float lox = own ? pi.x : 3.0e38f, loy = own ? pi.y : 3.0e38f, loz = own ? pi.z : 3.0e38f;
+        float hix = own ? pi.x : -3.0e38f, hiy = own ? pi.y : -3.0e38f, hiz = own ? pi.z : -3.0e38f;
+        for (int o = 16; o > 0; o >>= 1) {
+            lox = fminf(lox, __shfl_xor_sync(0xffffffffu, lox, o));
+            loy = fminf(loy, __shfl_xor_sync(0xffffffffu, loy, o));
+            loz = fminf(loz, __shfl_xor_sync(0xffffffffu, loz, o));
+            hix = fmaxf(hix, __shfl_xor_sync(0xffffffffu, hix, o));
+            hiy = fmaxf(hiy, __shfl_xor_sync(0xffffffffu, hiy, o));
+            hiz = fmaxf(hiz, __shfl_xor_sync(0xffffffffu, hiz, o));
+        }
+        const uint32_t self = (uint32_t)i | (13u << MD_CODE_SHIFT);
+        int cnt = 0, nb = 0, fill = 0;
         const int64_t il = own ? i : 0;
         uint32_t* row = IL ? nbr + il_block(il, 0, maxnb) * 8 : nbr + (size_t)il * maxnb;
         for (int oz = -1; oz <= 1; ++oz)
@@ -621,53 +682,57 @@ __device__ __forceinline__ void build_cell_rows(int64_t n, const float4* xl, con
                     const float shx = ox * g.side[0], shy = oy * g.side[1], shz = oz * g.side[2];
                     const int nb0 = start[cell], ne = start[cell + 1];
                     for (int j0 = nb0; j0 < ne; j0 += 32) {
-                        const int m = min(32, ne - j0);
-                        __syncwarp();
-                        if (lane < m) {
-                            const float4 pj = xl[j0 + lane];
-                            sx[lane] = -(pj.x + shx);
-                            sy[lane] = -(pj.y + shy);
-                            sz[lane] = -(pj.z + shz);
-                        } else {
-                            sx[lane] = 1e18f;
-                            sy[lane] = 1e18f;
-                            sz[lane] = 1e18f;
+                        const int jj = j0 + lane;
+                        bool keep = false;
+                        float x = 0.f, y = 0.f, z = 0.f;
+                        if (jj < ne) {
+                            const float4 pj = xl[jj];
+                            x = pj.x + shx;
+                            y = pj.y + shy;
+                            z = pj.z + shz;
+                            const float dx = fmaxf(fmaxf(lox - x, x - hix), 0.f);
+                            const float dy = fmaxf(fmaxf(loy - y, y - hiy), 0.f);
+                            const float dz = fmaxf(fmaxf(loz - z, z - hiz), 0.f);
+                            keep = dx * dx + dy * dy + dz * dz < pre2;
                         }
-                        __syncwarp();
-                        uint32_t hits = 0u;
-                        const int mm = (m + 1) & ~1;  // pairs of staged slots; slot m (if odd) is far away
-#pragma unroll 4
-                        for (int t = 0; t < mm; t += 2) {
-                            const float2 dx = __fadd2_rn(pix, *reinterpret_cast<const float2*>(sx + t));
-                            const float2 dy = __fadd2_rn(piy, *reinterpret_cast<const float2*>(sy + t));
-                            const float2 dz = __fadd2_rn(piz, *reinterpret_cast<const float2*>(sz + t));
-                            float2 r2 = __fmul2_rn(dz, dz);
-                            r2 = __ffma2_rn(dy, dy, r2);
-                            r2 = __ffma2_rn(dx, dx, r2);
-                            hits |= (r2.x < rl2 ? 1u : 0u) << t;
-                            hits |= (r2.y < rl2 ? 1u : 0u) << (t + 1);
+                        const uint32_t mk = __ballot_sync(0xffffffffu, keep);
+                        const int ck = __popc(mk), rank = __popc(mk & ((1u << lane) - 1u));
+                        const int room = 32 - fill;
+                        const uint32_t en = (uint32_t)jj | (code << MD_CODE_SHIFT);
+                        if (keep && rank < room) {
+                            sx[fill + rank] = -x;
+                            sy[fill + rank] = -y;
+                            sz[fill + rank] = -z;
+                            se[fill + rank] = en;
                         }
-                        if (!own) hits = 0u;
-                        if (i >= j0 && i < j0 + m) hits &= ~(1u << (i - j0));  // not the molecule itself
-                        const uint32_t e0 = (uint32_t)j0 | (code << MD_CODE_SHIFT);
-                        while (hits) {
-                            const int t = __ffs(hits) - 1;
-                            hits &= hits - 1u;
-                            buf[nb++] = e0 + (uint32_t)t;
-                            if (nb == BL_BUF) {
-                                if (cnt + BL_BUF <= maxnb) {
-                                    uint4* dst = reinterpret_cast<uint4*>(row + row_off<IL>(cnt));
-                                    dst[0] = make_uint4(buf[0], buf[1], buf[2], buf[3]);
-                                    dst[1] = make_uint4(buf[4], buf[5], buf[6], buf[7]);
-                                } else {
-                                    for (int u = 0; u < BL_BUF && cnt + u < maxnb; ++u) row[row_off<IL>(cnt + u)] = buf[u];
-                                }
-                                cnt += BL_BUF;
-                                nb = 0;
+                        if (ck >= room) {  // the staging area is full: test it, then stage the rest
+                            __syncwarp();
+                            test_staged<IL>(32, pix, piy, piz, rl2, sx, sy, sz, se, own, self, buf, nb, cnt, row,
+                                            maxnb);
+                            __syncwarp();
+                            if (keep && rank >= room) {
+                                sx[rank - room] = -x;
+                                sy[rank - room] = -y;
+                                sz[rank - room] = -z;
+                                se[rank - room] = en;
                             }
+                            fill = ck - room;
+                        } else {
+                            fill += ck;
                         }
                     }
                 }
+        // the last, partial staging area (unused slots far away)
+        __syncwarp();
+        if (lane >= fill) {
+            sx[lane] = 1e18f;
+            sy[lane] = 1e18f;
+            sz[lane] = 1e18f;
+        }
+        __syncwarp();
+        if (fill > 0)
+            test_staged<IL>(fill, pix, piy, piz, rl2, sx, sy, sz, se, own, self, buf, nb, cnt, row, maxnb);
+        __syncwarp();  // the next group reuses the staging area
         if (own) {
             for (int u = 0; u < nb && cnt + u < maxnb; ++u) row[row_off<IL>(cnt + u)] = buf[u];
             cnt += nb;
@@ -701,7 +766,7 @@ __global__ void __launch_bounds__(BL_WARPS * 32, 8) k_build_list(int64_t n, cons
                                                               float rl2, unsigned* status, int* need_max,
                                                               const unsigned* need) {
     if (!*need) return;
-    __shared__ __align__(16) float sq[BL_WARPS][3][32];
+    __shared__ __align__(16) float sq[BL_WARPS][4][32];
     __shared__ uint32_t sbuf[BL_WARPS][32][BL_BUF + 1];  // +1: no bank conflicts between lanes
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = blockIdx.x * BL_WARPS + wl;
