@@ -41,6 +41,12 @@
 //       calcFM, at the first force evaluation and in every step; force
 //       corrections applied to molecules with y in [y_lo, y_hi].  LRC
 //       records carry the step's UpotCorr and VirialCorr.
+//   res <file.inp> <rc> <rcLJ> <dt> <nsteps> <T> <prefix> <writefrequency> <accumulation_steps> <writeprecision>
+//       As `nvt` (T > 0) or `steps` (T = 0), with the reference's ResultWriter
+//       (io/ResultWriter.cpp) set up as its readXML would with these values:
+//       init() before the first step, endStep() after each step's global
+//       values and thermostat, the simulation time advanced by dt each step
+//       as Simulation::simulateOneTimestep does; writes <prefix>.res.
 //   steps <file.inp> <rc> <rcLJ> <dt> <nsteps>
 //       NVE Leapfrog steps with the periodic halo, in the order of the
 //       reference's Simulation::simulateOneTimestep (thermostat off, no
@@ -100,6 +106,7 @@
 #include "Simulation.h"
 #include "Domain.h"
 #include "longRange/Planar.h"
+#include "io/ResultWriter.h"
 #undef private
 #include "ensemble/EnsembleBase.h"
 #include "integrators/Leapfrog.h"
@@ -219,7 +226,8 @@ void forceStep(Setup& s, VectorizedCellProcessor& vcp) {
 	s.lc->deleteOuterParticles();
 }
 
-int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nsteps, double T = 0.0) {
+int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nsteps, double T = 0.0,
+			 ResultWriter* rw = nullptr) {
 	Setup s;
 	load(s, file, rc, rcLJ);
 	if (T > 0.0) {
@@ -239,6 +247,11 @@ int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nst
 	forceStep(s, vcp);
 	printGrid(s);
 	std::printf("STEP 0 %.17g %.17g nan nan\n", s.domain->getLocalUpot(), s.domain->getLocalVirial());
+	if (rw) {
+		global_simulation->_moleculeContainer = s.lc;  // the Domain counts molecules through it
+		s.domain->evaluateRho(s.lc->getNumberOfParticles(), s.dd);
+		rw->init(s.lc, s.dd, s.domain);
+	}
 	for (int k = 1; k <= nsteps; ++k) {
 		integrator.eventNewTimestep(s.lc, s.domain);
 		s.lc->update();
@@ -257,9 +270,27 @@ int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nst
 			thermostat.apply(s.lc);
 			std::printf("BETA %d %.17g %.17g\n", k, s.domain->getGlobalBetaTrans(), s.domain->getGlobalBetaRot());
 		}
+		if (rw) {
+			global_simulation->advanceSimulationTime(dt);  // Simulation::simulateOneTimestep, before the plugins' endStep
+			rw->endStep(s.lc, s.dd, s.domain, (unsigned long)k);
+		}
 	}
 	printMolecules(s);
 	return 0;
+}
+
+// ResultWriter::readXML's settings without an XML file.
+int runResults(const std::string& file, double rc, double rcLJ, double dt, int nsteps, double T,
+			   const std::string& prefix, int freq, int acc, int precision) {
+	ResultWriter rw;
+	rw._writeFrequency = freq;
+	rw._outputPrefix = prefix;
+	rw._U_pot_acc = std::make_unique<Accumulator<double>>(acc);
+	rw._U_kin_acc = std::make_unique<Accumulator<double>>(acc);
+	rw._p_acc = std::make_unique<Accumulator<double>>(acc);
+	rw._writePrecision = precision;
+	rw._writeWidth = precision + 15;
+	return runSteps(file, rc, rcLJ, dt, nsteps, T, &rw);
 }
 
 int runPlanar(const std::string& file, double rc, double rcLJ, double dt, int nsteps, int slabs, int freq,
@@ -427,6 +458,9 @@ int main(int argc, char** argv) {
 		return runBinWrite(argv[2], std::atof(argv[3]), argv[4], std::atof(argv[5]));
 	if (argc >= 6 && std::string(argv[1]) == "binr")
 		return runBinRead(argv[2], argv[3], argv[4], std::atof(argv[5]));
+	if (argc >= 12 && std::string(argv[1]) == "res")
+		return runResults(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]),
+						  std::atof(argv[7]), argv[8], std::atoi(argv[9]), std::atoi(argv[10]), std::atoi(argv[11]));
 	if (argc >= 7 && std::string(argv[1]) == "steps")
 		return runSteps(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]));
 	std::fprintf(stderr, "usage: %s forces <inp> <rc> <rcLJ> <periodic> | lrc <inp> <rc> <rcLJ> | steps <inp> <rc> <rcLJ> <dt> <n> | nvt <inp> <rc> <rcLJ> <dt> <n> <T> | binw <inp> <rc> <prefix> <time> | binr <inp> <header> <data> <rc>\n", argv[0]);
