@@ -65,9 +65,9 @@ BATCH_DESC = ("512 independent periodic 1CLJ boxes, N log-uniform in [500, 20000
 DEFAULT_SKIN = {"lj4m": 0.25, "lj1m": 0.25, "lj32k": 0.3, "slab": 0.25, "mix1m": 0.1}
 FLOP_PER_PAIR_LJ = 39.0  # reference FlopCounter model: 31 per LJ site pair + 8 per molecule distance
 # DRAM bytes (read + write) of one k_force_lj32x2 launch per pair-candidate list entry, from an ncu
-# capture of the 1,000,188-molecule case (598.9 MB for 100.2 entries per molecule); traffic grows
+# capture of the 1,000,188-molecule case (434.2 MB for 100.2 entries per molecule); traffic grows
 # with the entries read, so it is scaled by the live entry count.
-FORCE_DRAM_BYTES_PER_ENTRY = 598.9e6 / (1_000_188 * 100.2)
+FORCE_DRAM_BYTES_PER_ENTRY = 434.15e6 / (1_000_188 * 100.2)
 
 
 # ---------------------------------------------------------------- CUDA events on the engine stream
