@@ -493,6 +493,10 @@ def main():
 
     # ---- device-resident timing
     rmm = a.integrator == "rmm"
+    # md_run fuses Leapfrog's half steps into the pair kernel for one component of single-centre LJ molecules in
+    # mixed precision
+    fused = (a.precision == "mixed" and len(ps.components) == 1 and len(ps.components[0].lj) == 1
+             and not (ps.components[0].charges or ps.components[0].dipoles or ps.components[0].quadrupoles))
     mass = ps.components[0].lj[0].m if rmm else 1.0
 
     def first_forces(e):
@@ -572,9 +576,12 @@ def main():
                        "integrator": "LeapfrogRMM (reduced memory mode)" if rmm else "Leapfrog",
                        "parallelism": f"replicas x{world}", "l2": "working set > L2 (GBs), no flush needed"},
             # graph-captured chunks of 25 steps: the per-step kernels, the rebuild kernels of the steps that
-            # rebuilt the list, and one pre-force half step per chunk where it is fused into the post-force one
-            "gpu_launches": int(kt.launches_per_step * a.steps + kt.launches_per_rebuild * rebuilds_timed
-                                + (0 if rmm else -(-a.steps // 25))),
+            # rebuilt the list, and per chunk the half steps that are not fused (mixed single-centre LJ: the
+            # first pre-force and the last post-force half step; otherwise the first pre-force one); the reduced
+            # memory mode runs drift, rebuild test, pair kernel and two finalize launches per step
+            "gpu_launches": int((5 if rmm else kt.launches_per_step) * a.steps
+                                + kt.launches_per_rebuild * rebuilds_timed
+                                + (0 if rmm else (2 if fused else 1) * -(-a.steps // 25))),
             "roofline": {"bound": "hbm", "kernel": "k_force_lj32x2" if a.precision == "mixed" else "k_force_lj64",
                          "achieved": hbm_bytes / (kt.force_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                          "frac": hbm_bytes / (kt.force_ms * 1e-3) / 1e9 / hbm_peak,

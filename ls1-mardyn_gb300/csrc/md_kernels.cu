@@ -519,11 +519,13 @@ __global__ void k_permute(State dst, State src, const int* perm, const int* mcel
 // test) are stored per molecule; every pre-force step recomputes the local
 // coordinates from the FP64 position.  Slot n gets a position far outside
 // every box: candidate rows are padded with it.
-__global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, const unsigned* need) {
+__global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, const unsigned* need,
+                        float4* xl_other) {
     if (need && !*need) return;
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i == S.n) {  // the far-away slot that pads candidate rows
+    if (i == S.n) {  // the far-away slot that pads candidate rows (in both local-coordinate buffers)
         xlf[i] = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(0));
+        if (xl_other) xl_other[i] = xlf[i];
         return;
     }
     if (i > S.n) return;
@@ -1051,6 +1053,31 @@ __device__ __forceinline__ void lj_pack2(const float2 pix, const float2 piy, con
     a.nin = __fadd2_rn(a.nin, msk);
 }
 
+// Time-step constants of the half steps, computed on the host: dt/2 and
+// dt/(2m) per component, the latter with the same IEEE division the
+// reference performs per molecule (a device FP64 division costs about ten
+// FP64 instructions per molecule, and FP64 throughput bounds these kernels).
+struct Kick {
+    double dt, dt_halve;
+    double dtInv2m[MD_MAXC];
+    float massf[MD_MAXC];
+};
+
+// dt/(2m) of component c by selects over the parameter (a dynamic index
+// into a kernel parameter would copy it to local memory)
+__device__ __forceinline__ double kick_dtInv2m(const Kick& K, int c) {
+    double r = K.dtInv2m[0];
+#pragma unroll
+    for (int k = 1; k < MD_MAXC; ++k) r = c == k ? K.dtInv2m[k] : r;
+    return r;
+}
+__device__ __forceinline__ float kick_massf(const Kick& K, int c) {
+    float r = K.massf[0];
+#pragma unroll
+    for (int k = 1; k < MD_MAXC; ++k) r = c == k ? K.massf[k] : r;
+    return r;
+}
+
 // Single-component, single-LJ-centre molecules with rc_lj = rc (the 1CLJ
 // benchmarks), FP32 pair arithmetic on paired FP32 instructions.  One thread
 // per molecule streams its candidate row 16 bytes (four entries) at a time;
@@ -1067,9 +1094,25 @@ __device__ __forceinline__ void lj_pack2(const float2 pix, const float2 piy, con
 // is stored, the kick v += dt_inv_m F is applied at once (dt_inv_m = dt / m,
 // halved for the initial force pass), and with sum_v2 the kernel also
 // contributes sum v.v of the kicked velocities (VelocityCellProcessorRMM.h:
-// 95-128, no mass) to slot 12.
+// 95-128, no mass) to slot 12.  EPI_LEAPFROG is Leapfrog's post-force half
+// step of this step fused with the pre-force half step of the next (the
+// operations of k_post_pre in the same order; no force is stored): v and
+// sum m v^2 (slot 12) as k_post, then the kick, the drift r' = r + dt v into
+// the other position buffer (the near-cut-off FP64 decisions of other
+// molecules read this step's positions in the same launch) and the local
+// coordinates of r' into the other local-coordinate buffer, with the
+// displacement since the last list build.
 #define EPI_STORE 0
 #define EPI_RMM 1
+#define EPI_LEAPFROG 2
+struct LfStep {
+    Kick K;
+    double *rx, *ry, *rz;  // positions of the next step (written)
+    float4* xl;            // local coordinates of the next step (written)
+    const double* origin;
+    const float4* xlref;
+    unsigned* disp_max;
+};
 // v.v of the reduced mode's velocity sums (one expression for every kernel
 // that forms it, so their per-warp partials agree bit for bit)
 __device__ __forceinline__ double rmm_v2(double x, double y, double z) { return x * x + y * y + z * z; }
@@ -1080,7 +1123,8 @@ template <int EPI>
 __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State S, const float4* __restrict__ xlf,
                                                          const uint32_t* __restrict__ nbr,
                                                          const int* __restrict__ nnb, int maxnb, double* partials,
-                                                         int pstride, double dt_inv_m, int sum_v2) {
+                                                         int pstride, double dt_inv_m, int sum_v2, LfStep E) {
+    __shared__ float smax[8];
     // minus the offset of the neighbour cell's origin (code) from the home cell's origin, one table per
     // axis: three conflict-free 4-byte shared loads per candidate move fewer shared-memory wavefronts
     // than one 16-byte load (which also conflicts between codes 8 apart)
@@ -1094,7 +1138,8 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float up = 0.f, vir = 0.f, npairs = 0.f;  // halved per-molecule sums (every pair is seen twice)
-    float v2f = 0.f;                          // EPI_RMM: v.v after the kick
+    float v2f = 0.f;                          // EPI_RMM: v.v after the kick; EPI_LEAPFROG: m v.v
+    float d2 = 0.f;                           // EPI_LEAPFROG: squared displacement since the list build
     if (i < S.n) {
         const float4 p4 = xlf[i];
         const int gi = cP.comp[__float_as_int(p4.w)].ljoff;
@@ -1141,24 +1186,48 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
                 if (fp64_r2_canon(S, i, j, code) < cP.rclj2) lj_one(dx, dy, dz, r2, s2, fx, fy, fz, a);
             }
         }
-        // epilogue in FP32 (the precision of the pair sums) with exact conversions to the FP64 state
+        // epilogue in FP32 (the precision of the pair sums) with exact conversions to the FP64 state; the
+        // products are rounded on their own (no contraction into the sums below), so every epilogue variant
+        // forms the virial alike
         const float nin = a.nin.x + a.nin.y;
-        const float vx = e24 * (a.vx.x + a.vx.y), vy = e24 * (a.vy.x + a.vy.y), vz = e24 * (a.vz.x + a.vz.y);
+        const float vx = __fmul_rn(e24, a.vx.x + a.vx.y), vy = __fmul_rn(e24, a.vy.x + a.vy.y),
+                    vz = __fmul_rn(e24, a.vz.x + a.vz.y);
         if (EPI == EPI_STORE) {
             S.Fx[i] = f2d_exact(e24 * (fx.s - fx.c));
             S.Fy[i] = f2d_exact(e24 * (fy.s - fy.c));
             S.Fz[i] = f2d_exact(e24 * (fz.s - fz.c));
             S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
             S.Vx[i] = f2d_exact(0.5f * vx); S.Vy[i] = f2d_exact(0.5f * vy); S.Vz[i] = f2d_exact(0.5f * vz);
-        } else {
+        } else if (EPI == EPI_RMM) {
             const double ux = S.vx[i] + dt_inv_m * f2d_exact(e24 * (fx.s - fx.c));
             const double uy = S.vy[i] + dt_inv_m * f2d_exact(e24 * (fy.s - fy.c));
             const double uz = S.vz[i] + dt_inv_m * f2d_exact(e24 * (fz.s - fz.c));
             S.vx[i] = ux; S.vy[i] = uy; S.vz[i] = uz;
             const float gx = d2f_int(ux), gy = d2f_int(uy), gz = d2f_int(uz);
             v2f = gx * gx + (gy * gy + gz * gz);
+        } else {
+            const double F[3] = {f2d_exact(e24 * (fx.s - fx.c)), f2d_exact(e24 * (fy.s - fy.c)),
+                                 f2d_exact(e24 * (fz.s - fz.c))};
+            const double h = E.K.dtInv2m[0], dt = E.K.dt;  // one component
+            double v[3] = {S.vx[i], S.vy[i], S.vz[i]};
+            for (int d = 0; d < 3; ++d) v[d] += h * F[d];
+            const float gx = d2f_int(v[0]), gy = d2f_int(v[1]), gz = d2f_int(v[2]);
+            v2f = E.K.massf[0] * (gx * gx + (gy * gy + gz * gz));
+            for (int d = 0; d < 3; ++d) v[d] = v[d] + h * F[d];
+            const double rx = S.rx[i] + dt * v[0], ry = S.ry[i] + dt * v[1], rz = S.rz[i] + dt * v[2];
+            S.vx[i] = v[0]; S.vy[i] = v[1]; S.vz[i] = v[2];
+            E.rx[i] = rx; E.ry[i] = ry; E.rz[i] = rz;
+            const float4 q0 = E.xlref[i];
+            float4 p;
+            p.x = d2f_int(rx - E.origin[3 * i]);
+            p.y = d2f_int(ry - E.origin[3 * i + 1]);
+            p.z = d2f_int(rz - E.origin[3 * i + 2]);
+            p.w = q0.w;
+            E.xl[i] = p;
+            const float ddx = p.x - q0.x, ddy = p.y - q0.y, ddz = p.z - q0.z;
+            d2 = ddx * ddx + ddy * ddy + ddz * ddz;
         }
-        up = 0.5f * (e24 * (a.up.x + a.up.y) + sh6 * nin);
+        up = 0.5f * (__fmul_rn(e24, a.up.x + a.up.y) + __fmul_rn(sh6, nin));
         vir = 0.5f * (vx + (vy + vz));
         npairs = 0.5f * nin;
     }
@@ -1170,6 +1239,17 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
     warp_partial_count(partials, pstride, 5, npairs);
     for (int sl = 6; sl < 12; ++sl) warp_partial_zero(partials, pstride, sl);
     if (EPI == EPI_RMM && sum_v2) warp_partial_f32(partials, pstride, 12, v2f);
+    if (EPI == EPI_LEAPFROG) {
+        warp_partial_f32(partials, pstride, 12, v2f);
+        for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, o));
+        if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = d2;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float m = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, smax[w]);
+            atomicMax(E.disp_max, __float_as_uint(m));
+        }
+    }
 }
 
 // FP64 variant: absolute FP64 positions with the reference's halo image
@@ -1526,34 +1606,12 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
 }
 
 // ------------------------------------------------------------------ integration
-// Time-step constants of the half steps, computed on the host: dt/2 and
-// dt/(2m) per component, the latter with the same IEEE division the
-// reference performs per molecule (a device FP64 division costs about ten
-// FP64 instructions per molecule, and FP64 throughput bounds these kernels).
-struct Kick {
-    double dt, dt_halve;
-    double dtInv2m[MD_MAXC];
-    float massf[MD_MAXC];
-};
-
-// dt/(2m) of component c by selects over the parameter (a dynamic index
-// into a kernel parameter would copy it to local memory)
-__device__ __forceinline__ double kick_dtInv2m(const Kick& K, int c) {
-    double r = K.dtInv2m[0];
-#pragma unroll
-    for (int k = 1; k < MD_MAXC; ++k) r = c == k ? K.dtInv2m[k] : r;
-    return r;
-}
-__device__ __forceinline__ float kick_massf(const Kick& K, int c) {
-    float r = K.massf[0];
-#pragma unroll
-    for (int k = 1; k < MD_MAXC; ++k) r = c == k ? K.massf[k] : r;
-    return r;
-}
-
 // FullMolecule::upd_preF; afterwards the FP32 local coordinates and the
 // displacement since the last list build (for the rebuild test).
-__global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const float4* xlref, unsigned* disp_max) {
+// The positions are written to rxo/ryo/rzo (the state's own arrays, or the
+// other position buffer of md_run's fused steps).
+__global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const float4* xlref, unsigned* disp_max,
+                      double* rxo, double* ryo, double* rzo) {
     __shared__ float smax[8];
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float d2 = 0.f;
@@ -1567,7 +1625,7 @@ __global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const 
         double vz = S.vz[i] + dtInv2m * S.Fz[i];
         double rx = S.rx[i] + dt * vx, ry = S.ry[i] + dt * vy, rz = S.rz[i] + dt * vz;
         S.vx[i] = vx; S.vy[i] = vy; S.vz[i] = vz;
-        S.rx[i] = rx; S.ry[i] = ry; S.rz[i] = rz;
+        rxo[i] = rx; ryo[i] = ry; rzo[i] = rz;
         if (!C.skip_rot) {
             double q[4] = {S.qw[i], S.qx[i], S.qy[i], S.qz[i]};
             double L[3] = {S.Lx[i], S.Ly[i], S.Lz[i]};
@@ -1655,6 +1713,18 @@ __global__ void k_rmm_vsum(State S, double* partials, int pstride) {
     double v2 = 0.0;
     if (i < S.n) v2 = rmm_v2(S.vx[i], S.vy[i], S.vz[i]);
     warp_partial(partials, pstride, 12, v2);
+}
+
+// Copy of the three position arrays (the rebuilt master state into the
+// other position buffer of md_run's fused steps).
+__global__ void k_copy_r(const double* ax, const double* ay, const double* az, double* bx, double* by, double* bz,
+                         int64_t n, const unsigned* need) {
+    if (need && !*need) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        bx[i] = ax[i];
+        by[i] = ay[i];
+        bz[i] = az[i];
+    }
 }
 
 // Rebuild when two molecules may have approached by more than the skin.

@@ -152,6 +152,39 @@ def test_step_by_step_equals_md_run(engine_mod):
     assert np.allclose(np.array(manual), rec[:, :3], rtol=1e-12, atol=0)
 
 
+def test_fused_leapfrog_steps_equal_step_by_step(engine_mod):
+    """Mixed precision, one component of single-centre LJ molecules: md_run
+    fuses the post-force half step of each step and the pre-force half step
+    of the next into the pair kernel (two position buffers).  60 steps (two
+    graph-captured chunks and an eager remainder, several list rebuilds)
+    against md_integrate_pre / md_compute_forces / md_integrate_post: the same
+    FP64 operations, so positions, velocities, Upot and virial agree bit for
+    bit; the kinetic sums are FP32 products in the fused kernel (1e-6)."""
+    ps, g = golden_io.load("per_lj500")
+    rng = np.random.default_rng(5)
+    ps.v = ps.v * 1.5 + rng.normal(0.0, 0.2, ps.v.shape)
+    cells = engine_mod.GpuLinkedCells(ps, 2.5, precision="mixed", skin=0.2)
+    lf = engine_mod.GpuLeapfrog(0.004)
+    cells.traverseCells()
+    manual = []
+    for _ in range(60):
+        lf.eventNewTimestep(cells)
+        fo = cells.traverseCells()
+        ko = lf.eventForcesCalculated(cells)
+        manual.append([fo.upot, fo.virial, ko.summv2])
+    manual = np.array(manual)
+    e = engine_mod.Engine(ps, 2.5, precision="mixed", skin=0.2)
+    e.forces()
+    rec = e.run(0.004, 60)
+    a, b = cells.molecules(), e.molecules()
+    assert e.rebuilds() >= 3
+    e.close()
+    np.testing.assert_array_equal(rec[:, :2], manual[:, :2])
+    assert np.abs(rec[:, 2] - manual[:, 2]).max() <= 1e-6 * np.abs(manual[:, 2]).max()
+    for k in ("ids", "r", "v", "F"):
+        np.testing.assert_array_equal(a[k], b[k])
+
+
 def test_mixed_matches_fp64_at_scale(engine_mod):
     """1CLJ N=32000 (the reference's small benchmark case): mixed-precision
     forces within 1e-5 relative rms of the FP64 kernel, Upot within 1e-6."""
