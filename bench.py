@@ -68,6 +68,12 @@ FLOP_PER_PAIR_LJ = 39.0  # reference FlopCounter model: 31 per LJ site pair + 8 
 # capture of the 1,000,188-molecule case (434.2 MB for 100.2 entries per molecule); traffic grows
 # with the entries read, so it is scaled by the live entry count.
 FORCE_DRAM_BYTES_PER_ENTRY = 434.15e6 / (1_000_188 * 100.2)
+# The same for the pair kernel with both Leapfrog half steps fused (md_run's steps of one component of
+# single-centre LJ molecules in mixed precision): 518.4 MB for 105.5 entries per molecule at 1,000,188.
+STEP_DRAM_BYTES_PER_ENTRY = 518.4e6 / (1_000_188 * 105.47)
+# algorithmic bytes per molecule of that kernel beyond the list entries: position 16, count 4, r and v read
+# and written 4 x 24, home-cell origin 24, local coordinates at the list build 16, next local coordinates 16
+STEP_BYTES_PER_MOLECULE = 16 + 4 + 4 * 24 + 24 + 16 + 16
 
 
 # ---------------------------------------------------------------- CUDA events on the engine stream
@@ -528,10 +534,25 @@ def main():
     pairs = fo.site_pairs[0]
     flops = FLOP_PER_PAIR_LJ * pairs
     fp32_peak = 152 * 128 * 2 * 2070e6 / 1e12   # TFLOP/s at the maximum SM clock
-    achieved = flops / (kt.force_ms * 1e-3) / 1e12
     list_bytes = kt.mean_candidates * n * 4.0
-    hbm_bytes = list_bytes + n * (16 + 4 + 9 * 8)
-    traffic = FORCE_DRAM_BYTES_PER_ENTRY * kt.mean_candidates * n if a.precision == "mixed" else None
+    # the dominant kernel of the timed steps: in the fused Leapfrog steps the pair kernel that also runs
+    # both half steps, else the plain pair kernel
+    step_kernel = fused and not rmm and kt.step_force_ms > 0
+    if step_kernel:
+        kname = "k_force_lj32x2<EPI_LEAPFROG> (pair kernel with both Leapfrog half steps)"
+        launch_ms = kt.step_force_ms
+        hbm_bytes = list_bytes + n * STEP_BYTES_PER_MOLECULE
+        alg_desc = ("per launch: 4 B per pair-candidate list entry + 16 B position + 4 B count + 152 B Leapfrog "
+                    "state per molecule (r and v read and written, home-cell origin, list-build and next local "
+                    "coordinates)")
+        traffic = STEP_DRAM_BYTES_PER_ENTRY * kt.mean_candidates * n
+    else:
+        kname = "k_force_lj32x2" if a.precision == "mixed" else "k_force_lj64"
+        launch_ms = kt.force_ms
+        hbm_bytes = list_bytes + n * (16 + 4 + 9 * 8)
+        alg_desc = "per launch: 4 B per pair-candidate list entry + 16 B position + 4 B count + 72 B F/M/Vi per molecule"
+        traffic = FORCE_DRAM_BYTES_PER_ENTRY * kt.mean_candidates * n if a.precision == "mixed" else None
+    achieved = flops / (launch_ms * 1e-3) / 1e12
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     hbm_peak, hbm_src = 6800.0, "fallback"
     if os.path.exists(peaks_path):
@@ -582,18 +603,17 @@ def main():
             "gpu_launches": int((5 if rmm else kt.launches_per_step) * a.steps
                                 + kt.launches_per_rebuild * rebuilds_timed
                                 + (0 if rmm else (2 if fused else 1) * -(-a.steps // 25))),
-            "roofline": {"bound": "hbm", "kernel": "k_force_lj32x2" if a.precision == "mixed" else "k_force_lj64",
-                         "achieved": hbm_bytes / (kt.force_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": hbm_bytes / (kt.force_ms * 1e-3) / 1e9 / hbm_peak,
+            "roofline": {"bound": "hbm", "kernel": kname,
+                         "achieved": hbm_bytes / (launch_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": hbm_bytes / (launch_ms * 1e-3) / 1e9 / hbm_peak,
                          "traffic": traffic, "peak_source": hbm_src,
-                         "algorithmic": "per launch: 4 B per pair-candidate list entry + 16 B position + 4 B count"
-                                        " + 72 B F/M/Vi per molecule",
-                         "algorithmic_bytes": hbm_bytes, "launch_ms": kt.force_ms},
+                         "algorithmic": alg_desc, "algorithmic_bytes": hbm_bytes, "launch_ms": launch_ms},
             "roofline_fp32": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                               "frac": achieved / fp32_peak,
                               "algorithmic": f"{FLOP_PER_PAIR_LJ:.0f} flop x {pairs} unique in-cutoff pairs per launch",
                               "peak_source": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 flop x 2070 MHz"},
-            "kernels_ms": {"force": kt.force_ms, "pre": kt.pre_ms, "post": kt.post_ms, "rebuild": kt.rebuild_ms},
+            "kernels_ms": {"force": kt.force_ms, "force_with_both_half_steps": kt.step_force_ms, "pre": kt.pre_ms,
+                           "post": kt.post_ms, "rebuild": kt.rebuild_ms},
             "pair_list": {"mean_candidates": kt.mean_candidates, "rebuilds": int(kt.rebuilds),
                           "rebuilds_timed": int(rebuilds_timed)},
             "physics": {"upot_per_molecule": fo.upot / n, "unique_lj_pairs": int(pairs)},

@@ -314,6 +314,9 @@ typedef struct {
     int32_t launches_per_rebuild; /* kernels a list rebuild adds to such a step         */
     double adjoint_ms;        /* one md_adjoint kernel pass (gU = gW = 1, no gF),
                                  without its host copies                                */
+    double step_force_ms;     /* one pair kernel with both Leapfrog half steps fused, as
+                                 md_run runs it for one component of single-centre LJ
+                                 molecules in mixed precision; 0 otherwise              */
 } md_kernel_times;
 
 int md_get_stream(md_ctx* ctx, void** stream);

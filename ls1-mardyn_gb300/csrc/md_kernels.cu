@@ -501,15 +501,19 @@ __global__ void k_cell_sort(const int* start, int ncells, int* perm, const int* 
     }
 }
 
-// Gather all master arrays into slot order (dst = src[perm]).
-__global__ void k_permute(State dst, State src, const int* perm, const int* mcell, const unsigned* need) {
+// Gather all master arrays into slot order (dst = src[perm]); the force
+// outputs F, M, Vi only with `outputs`.
+__global__ void k_permute(State dst, State src, const int* perm, const int* mcell, const unsigned* need, int outputs) {
     if (!*need) return;
     int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= src.n) return;
     int64_t i = perm[k];
 #define PM(a) dst.a[k] = src.a[i]
     PM(rx); PM(ry); PM(rz); PM(vx); PM(vy); PM(vz); PM(qw); PM(qx); PM(qy); PM(qz); PM(Lx); PM(Ly); PM(Lz);
-    PM(Fx); PM(Fy); PM(Fz); PM(Mx); PM(My); PM(Mz); PM(Vx); PM(Vy); PM(Vz); PM(comp); PM(orig); PM(id);
+    if (outputs) {
+        PM(Fx); PM(Fy); PM(Fz); PM(Mx); PM(My); PM(Mz); PM(Vx); PM(Vy); PM(Vz);
+    }
+    PM(comp); PM(orig); PM(id);
 #undef PM
     dst.home[k] = mcell[i];
 }

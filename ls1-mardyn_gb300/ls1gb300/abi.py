@@ -73,7 +73,7 @@ class MdKernelTimes(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("pre_ms", C.c_double), ("post_ms", C.c_double),
                 ("rebuild_ms", C.c_double), ("mean_candidates", C.c_double), ("rebuilds", C.c_int64),
                 ("launches_per_step", C.c_int32), ("launches_per_rebuild", C.c_int32),
-                ("adjoint_ms", C.c_double)]
+                ("adjoint_ms", C.c_double), ("step_force_ms", C.c_double)]
 
 
 class MdBatchConfig(C.Structure):
