@@ -599,10 +599,12 @@ def main():
             # graph-captured chunks of 25 steps: the per-step kernels, the rebuild kernels of the steps that
             # rebuilt the list, and per chunk the half steps that are not fused (mixed single-centre LJ: the
             # first pre-force and the last post-force half step; otherwise the first pre-force one); the reduced
-            # memory mode runs drift, rebuild test, pair kernel and two finalize launches per step
-            "gpu_launches": int((5 if rmm else kt.launches_per_step) * a.steps
+            # memory mode runs rebuild test, pair kernel and two finalize launches per step, with the drift in
+            # the pair kernel but for the first step of a chunk in mixed precision, as a kernel of its own in FP64
+            "gpu_launches": int(((4 if a.precision == "mixed" else 5) if rmm else kt.launches_per_step) * a.steps
                                 + kt.launches_per_rebuild * rebuilds_timed
-                                + (0 if rmm else (2 if fused else 1) * -(-a.steps // 25))),
+                                + ((1 if a.precision == "mixed" else 0) if rmm else (2 if fused else 1))
+                                * -(-a.steps // 25)),
             "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": hbm_bytes / (launch_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                          "frac": hbm_bytes / (launch_ms * 1e-3) / 1e9 / hbm_peak,

@@ -1109,6 +1109,10 @@ __device__ __forceinline__ float kick_massf(const Kick& K, int c) {
 #define EPI_STORE 0
 #define EPI_RMM 1
 #define EPI_LEAPFROG 2
+// EPI_RMM_DRIFT: EPI_RMM followed by the next step's drift r' = r + dt v
+// (PositionCellProcessorRMM) into the other position buffer, as EPI_LEAPFROG
+// writes its drift (dt = E.K.dt).
+#define EPI_RMM_DRIFT 3
 struct LfStep {
     Kick K;
     double *rx, *ry, *rz;  // positions of the next step (written)
@@ -1202,13 +1206,27 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
             S.Fz[i] = f2d_exact(e24 * (fz.s - fz.c));
             S.Mx[i] = 0.0; S.My[i] = 0.0; S.Mz[i] = 0.0;
             S.Vx[i] = f2d_exact(0.5f * vx); S.Vy[i] = f2d_exact(0.5f * vy); S.Vz[i] = f2d_exact(0.5f * vz);
-        } else if (EPI == EPI_RMM) {
+        } else if (EPI == EPI_RMM || EPI == EPI_RMM_DRIFT) {
             const double ux = S.vx[i] + dt_inv_m * f2d_exact(e24 * (fx.s - fx.c));
             const double uy = S.vy[i] + dt_inv_m * f2d_exact(e24 * (fy.s - fy.c));
             const double uz = S.vz[i] + dt_inv_m * f2d_exact(e24 * (fz.s - fz.c));
             S.vx[i] = ux; S.vy[i] = uy; S.vz[i] = uz;
             const float gx = d2f_int(ux), gy = d2f_int(uy), gz = d2f_int(uz);
             v2f = gx * gx + (gy * gy + gz * gz);
+            if (EPI == EPI_RMM_DRIFT) {
+                const double dt = E.K.dt;
+                const double rx = S.rx[i] + dt * ux, ry = S.ry[i] + dt * uy, rz = S.rz[i] + dt * uz;
+                E.rx[i] = rx; E.ry[i] = ry; E.rz[i] = rz;
+                const float4 q0 = E.xlref[i];
+                float4 p;
+                p.x = d2f_int(rx - E.origin[3 * i]);
+                p.y = d2f_int(ry - E.origin[3 * i + 1]);
+                p.z = d2f_int(rz - E.origin[3 * i + 2]);
+                p.w = q0.w;
+                E.xl[i] = p;
+                const float ddx = p.x - q0.x, ddy = p.y - q0.y, ddz = p.z - q0.z;
+                d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+            }
         } else {
             const double F[3] = {f2d_exact(e24 * (fx.s - fx.c)), f2d_exact(e24 * (fy.s - fy.c)),
                                  f2d_exact(e24 * (fz.s - fz.c))};
@@ -1242,9 +1260,9 @@ __global__ void __launch_bounds__(256, MD_LJX2_MIN_BLOCKS) k_force_lj32x2(State 
     warp_partial_count(partials, pstride, 4, npairs);
     warp_partial_count(partials, pstride, 5, npairs);
     for (int sl = 6; sl < 12; ++sl) warp_partial_zero(partials, pstride, sl);
-    if (EPI == EPI_RMM && sum_v2) warp_partial_f32(partials, pstride, 12, v2f);
-    if (EPI == EPI_LEAPFROG) {
-        warp_partial_f32(partials, pstride, 12, v2f);
+    if ((EPI == EPI_RMM || EPI == EPI_RMM_DRIFT) && sum_v2) warp_partial_f32(partials, pstride, 12, v2f);
+    if (EPI == EPI_LEAPFROG || EPI == EPI_RMM_DRIFT) {
+        if (EPI == EPI_LEAPFROG) warp_partial_f32(partials, pstride, 12, v2f);
         for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, o));
         if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = d2;
         __syncthreads();
@@ -1680,16 +1698,17 @@ __global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const 
 
 // Reduced memory mode, PositionCellProcessorRMM::processCell
 // (PositionCellProcessorRMM.h:33-60): r += dt v for every molecule, nothing
-// else; then the FP32 local coordinates and the displacement since the last
-// list build, as in k_pre.
+// else (written to rxo/ryo/rzo: the state's own arrays, or the other position
+// buffer of md_rmm_run's fused steps); then the FP32 local coordinates and the
+// displacement since the last list build, as in k_pre.
 __global__ void k_rmm_drift(State S, double dt, float4* xlf, const double* origin, const float4* xlref,
-                            unsigned* disp_max) {
+                            unsigned* disp_max, double* rxo, double* ryo, double* rzo) {
     __shared__ float smax[8];
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float d2 = 0.f;
     if (i < S.n) {
         const double rx = S.rx[i] + dt * S.vx[i], ry = S.ry[i] + dt * S.vy[i], rz = S.rz[i] + dt * S.vz[i];
-        S.rx[i] = rx; S.ry[i] = ry; S.rz[i] = rz;
+        rxo[i] = rx; ryo[i] = ry; rzo[i] = rz;
         const float4 q0 = xlref[i];
         float4 p;
         p.x = d2f_int(rx - origin[3 * i]);

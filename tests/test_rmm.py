@@ -165,6 +165,41 @@ def test_rmm_calls_equal_run(engine_mod):
 
 
 @pytest.mark.gpu
+def test_rmm_mixed_fused_drift_equals_calls(engine_mod):
+    """Mixed precision: md_rmm_run puts the next step's drift into the pair
+    kernel (two position buffers).  60 steps (two graph chunks and an eager
+    remainder, several rebuilds) against the drift / force / velocity calls:
+    positions, velocities, Upot and virial bit for bit; the velocity sums are
+    FP32 products in the fused kernel (1e-6)."""
+    ps = _lj_box(cells=7, mass=1.0)
+    ps.v = ps.v * 1.5
+    dt, n = 0.004, 60
+    a = engine_mod.Engine(ps, 2.5, precision="mixed", skin=0.2)
+    b = engine_mod.Engine(ps, 2.5, precision="mixed", skin=0.2)
+    ra = engine_mod.GpuLinkedCells.__new__(engine_mod.GpuLinkedCells)
+    ra.engine, ra._cutoff = a, 2.5
+    integ = engine_mod.GpuLeapfrogRMM(dt, 1.0)
+    integ.prepare(ra)
+    rows = []
+    for _ in range(n):
+        integ.eventNewTimestep(ra)
+        fo = integ.traverseCells(ra)
+        ko = integ.eventForcesCalculated(ra)
+        rows.append([fo.upot, fo.virial, ko.summv2])
+    rows = np.array(rows)
+    b.rmm_forces(0.5 * dt)
+    rec = b.rmm_run(dt, n)
+    assert b.rebuilds() >= 3
+    ma, mb = a.molecules(), b.molecules()
+    a.close()
+    b.close()
+    np.testing.assert_array_equal(rec[:, :2], rows[:, :2])
+    assert np.abs(rec[:, 2] - rows[:, 2]).max() <= 1e-6 * np.abs(rows[:, 2]).max()
+    for k in ("ids", "r", "v"):
+        np.testing.assert_array_equal(ma[k], mb[k])
+
+
+@pytest.mark.gpu
 def test_rmm_positions_follow_leapfrog_at_scale(engine_mod):
     """108,000 molecules, 40 steps: the reduced mode's positions, Upot and
     virial are the Leapfrog ones (FP64, same list schedule up to rounding)."""
