@@ -271,6 +271,47 @@ int md_set_thermostats(md_ctx* ctx, const int32_t* component_thermostat, int32_t
                        const double* target_temperatures, int32_t explosion_heuristics);
 int md_thermostat_betas(md_ctx* ctx, int32_t thermostat, double* beta_trans, double* beta_rot);
 
+/* Region-wise temperature control (thermostats/TemperatureControl: velocity
+ * scaling per control region and slab).  A region is the open box lower <
+ * r < upper; its molecules of `component` (1-based; 0 = all) are binned in
+ * `numslabs` slabs along y.  Every `frequency`-th step with start < step <
+ * stop (Init/MeasureKineticEnergy/CalcGlobalValues) the sums per slab give
+ * beta_trans = (ndir N T / sum m v_d^2)^exponent over the thermostated
+ * directions d (bits 1 = x, 2 = y, 4 = z) and beta_rot = (rotDOF T / sum I
+ * w^2)^exponent (1 for an empty slab or no rotational DOF); for start < step
+ * <= stop (ControlTemperature) those directions of v are scaled by 2 -
+ * 1/beta_trans and L by 2 - 1/beta_rot, region by region
+ * (TemperatureControl.cpp:241-427, 666-770).  T follows the region's ramp
+ * (start -> end between update_start and update_stop, every update_freq
+ * steps) when ramp_enabled.  Replaces the global and component-wise
+ * thermostats inside md_run (Simulation.cpp:1236-1268), applied after each
+ * step's global values; md_set_simstep sets the step number of the state
+ * (md_run's steps are step + 1, step + 2, ...).  md_temperature_control_betas
+ * reads the betas of region r's slabs of the last measurement; the Andersen
+ * method of TemperatureControl is not offered. */
+#define MD_TC_MAX_REGIONS 8
+#define MD_TC_MAX_SLABS 64
+typedef struct {
+    double lower[3], upper[3];
+    double target_temperature;
+    int32_t component;          /* 1-based component id, 0 = every component */
+    int32_t numslabs;           /* 1 .. MD_TC_MAX_SLABS                        */
+    double exponent;
+    int32_t directions;         /* bit mask: 1 = x, 2 = y, 4 = z               */
+    int32_t ramp_enabled;
+    double ramp_start, ramp_end;
+    int64_t ramp_update_start, ramp_update_stop, ramp_update_freq;
+} md_tc_region;
+typedef struct {
+    int64_t start, frequency, stop;
+    int32_t nregions;
+    int32_t reserved;
+    md_tc_region regions[MD_TC_MAX_REGIONS];
+} md_temperature_control;
+int md_set_temperature_control(md_ctx* ctx, const md_temperature_control* tc);
+int md_set_simstep(md_ctx* ctx, int64_t simstep);
+int md_temperature_control_betas(md_ctx* ctx, int32_t region, double* beta_trans, double* beta_rot);
+
 /* Wait for all work of the context. */
 int md_sync(md_ctx* ctx);
 

@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libls1gb300.so")
 SOURCES = ["md_kernels.cu", "md_static.cu"]
-DEPS = ["md_kernels.cu", "md_api.inc", "md_device.cuh", "md_pair.cuh", "md_batch.inc", "md_adjoint.inc", "md_planar.inc", "md_static.cu"]
+DEPS = ["md_kernels.cu", "md_api.inc", "md_device.cuh", "md_pair.cuh", "md_batch.inc", "md_adjoint.inc", "md_planar.inc", "md_tempctl.inc", "md_static.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

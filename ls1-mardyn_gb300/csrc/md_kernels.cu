@@ -1874,4 +1874,5 @@ __global__ void k_post_pre(State S, Kick K, double* partials, int pstride, float
 #include "md_adjoint.inc"
 #include "md_api.inc"
 #include "md_planar.inc"
+#include "md_tempctl.inc"
 #include "md_batch.inc"

@@ -65,6 +65,23 @@ class MdPlanarConfig(C.Structure):
                 ("target_temperature", C.c_double)]
 
 
+MD_TC_MAX_REGIONS = 8
+MD_TC_MAX_SLABS = 64
+
+
+class MdTcRegion(C.Structure):
+    _fields_ = [("lower", C.c_double * 3), ("upper", C.c_double * 3), ("target_temperature", C.c_double),
+                ("component", C.c_int32), ("numslabs", C.c_int32), ("exponent", C.c_double),
+                ("directions", C.c_int32), ("ramp_enabled", C.c_int32), ("ramp_start", C.c_double),
+                ("ramp_end", C.c_double), ("ramp_update_start", C.c_int64), ("ramp_update_stop", C.c_int64),
+                ("ramp_update_freq", C.c_int64)]
+
+
+class MdTemperatureControl(C.Structure):
+    _fields_ = [("start", C.c_int64), ("frequency", C.c_int64), ("stop", C.c_int64), ("nregions", C.c_int32),
+                ("reserved", C.c_int32), ("regions", MdTcRegion * MD_TC_MAX_REGIONS)]
+
+
 class MdStepRecord(C.Structure):
     _fields_ = [("upot", C.c_double), ("virial", C.c_double), ("summv2", C.c_double), ("sumIw2", C.c_double)]
 

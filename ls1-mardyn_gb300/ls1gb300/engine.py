@@ -72,6 +72,9 @@ def load_library(path: str = LIB_PATH):
     L.md_apply_thermostat.argtypes = [vp, dp, dp]
     L.md_set_thermostats.argtypes = [vp, vp, i32, dp, i32]
     L.md_thermostat_betas.argtypes = [vp, i32, dp, dp]
+    L.md_set_temperature_control.argtypes = [vp, C.POINTER(abi.MdTemperatureControl)]
+    L.md_set_simstep.argtypes = [vp, i64]
+    L.md_temperature_control_betas.argtypes = [vp, i32, dp, dp]
     L.md_planar_init.argtypes = [vp, C.POINTER(abi.MdPlanarConfig)]
     L.md_planar_apply.argtypes = [vp, dp, dp]
     L.md_write_phasespace_binary.argtypes = [vp, C.c_char_p, d]
@@ -231,6 +234,43 @@ class Engine:
         t = np.ascontiguousarray(targets, np.float64)
         self._check(self.L.md_set_thermostats(self.h, m.ctypes.data, len(t), abi.dptr(t), int(explosion_heuristics)),
                     "md_set_thermostats")
+
+    def set_temperature_control(self, tc: Optional[dict]):
+        """Region-wise temperature control (TemperatureControl with velocity-scaling regions).  ``tc``:
+        start, frequency, stop and a list of regions with lower/upper corners (an upper corner None is the
+        box length, as the reference's "box"), T, component (1-based, 0 = all), numslabs, exponent,
+        directions (bit mask x = 1, y = 2, z = 4) and an optional ramp (start, end, update_start,
+        update_stop, update_freq).  None switches it off."""
+        if tc is None:
+            self._check(self.L.md_set_temperature_control(self.h, None), "md_set_temperature_control")
+            return
+        c = abi.MdTemperatureControl()
+        c.start, c.frequency, c.stop = int(tc["start"]), int(tc["frequency"]), int(tc["stop"])
+        c.nregions = len(tc["regions"])
+        for k, r in enumerate(tc["regions"]):
+            g = c.regions[k]
+            for d in range(3):
+                g.lower[d] = float(r["lower"][d])
+                g.upper[d] = float(self.ps.box[d] if r["upper"][d] is None else r["upper"][d])
+            g.target_temperature = float(r["T"])
+            g.component, g.numslabs = int(r["component"]), int(r["numslabs"])
+            g.exponent, g.directions = float(r["exponent"]), int(r["directions"])
+            ramp = r.get("ramp")
+            g.ramp_enabled = 1 if ramp else 0
+            if ramp:
+                g.ramp_start, g.ramp_end = float(ramp["start"]), float(ramp["end"])
+                g.ramp_update_start, g.ramp_update_stop = int(ramp["update_start"]), int(ramp["update_stop"])
+                g.ramp_update_freq = int(ramp["update_freq"])
+        self._check(self.L.md_set_temperature_control(self.h, C.byref(c)), "md_set_temperature_control")
+
+    def set_simstep(self, step: int):
+        self._check(self.L.md_set_simstep(self.h, int(step)), "md_set_simstep")
+
+    def temperature_control_betas(self, region: int, numslabs: int):
+        bt, br = np.zeros(numslabs), np.zeros(numslabs)
+        self._check(self.L.md_temperature_control_betas(self.h, int(region), abi.dptr(bt), abi.dptr(br)),
+                    "md_temperature_control_betas")
+        return bt, br
 
     def thermostat_betas(self, thermostat: int = 0):
         bt, br = C.c_double(), C.c_double()

@@ -47,6 +47,14 @@
 //       init() before the first step, endStep() after each step's global
 //       values and thermostat, the simulation time advanced by dt each step
 //       as Simulation::simulateOneTimestep does; writes <prefix>.res.
+//   tc <file.inp> <rc> <rcLJ> <dt> <nsteps> <tc.xml>
+//       As `steps`, with the reference's TemperatureControl read from the
+//       <temperatureControl> element of tc.xml (TemperatureControl::readXML,
+//       prepare_start) and DoLoopsOverMolecules(simstep = k) after each
+//       step's global values, where Simulation::simulateOneTimestep calls it.
+//       TCB records carry <k> <region> <slab> <beta_trans> <beta_rot> <N>
+//       after each measuring step.  Writes the reference's beta and added
+//       kinetic energy logs into the working directory.
 //   steps <file.inp> <rc> <rcLJ> <dt> <nsteps>
 //       NVE Leapfrog steps with the periodic halo, in the order of the
 //       reference's Simulation::simulateOneTimestep (thermostat off, no
@@ -127,6 +135,11 @@
 #undef private
 
 static_assert(VCP_VEC_TYPE == VCP_NOVEC, "golden vectors come from the scalar kernel path");
+
+// TemperatureControl lives in ref_harness_tc.cpp: its header declares a class
+// Accumulator that clashes with the ResultWriter's utils/Accumulator.h.
+void* harnessTcCreate(const char* xml);
+void harnessTcStep(void* tc, DomainDecompBase* dd, ParticleContainer* lc, unsigned long k);
 
 namespace {
 
@@ -227,9 +240,10 @@ void forceStep(Setup& s, VectorizedCellProcessor& vcp) {
 }
 
 int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nsteps, double T = 0.0,
-			 ResultWriter* rw = nullptr) {
+			 ResultWriter* rw = nullptr, const char* tcXml = nullptr) {
 	Setup s;
 	load(s, file, rc, rcLJ);
+	void* tc = tcXml ? harnessTcCreate(tcXml) : nullptr;
 	if (T > 0.0) {
 		s.domain->thermostatOn();
 		s.domain->setGlobalTemperature(T);
@@ -270,6 +284,7 @@ int runSteps(const std::string& file, double rc, double rcLJ, double dt, int nst
 			thermostat.apply(s.lc);
 			std::printf("BETA %d %.17g %.17g\n", k, s.domain->getGlobalBetaTrans(), s.domain->getGlobalBetaRot());
 		}
+		if (tc) harnessTcStep(tc, s.dd, s.lc, (unsigned long)k);
 		if (rw) {
 			global_simulation->advanceSimulationTime(dt);  // Simulation::simulateOneTimestep, before the plugins' endStep
 			rw->endStep(s.lc, s.dd, s.domain, (unsigned long)k);
@@ -461,6 +476,9 @@ int main(int argc, char** argv) {
 	if (argc >= 12 && std::string(argv[1]) == "res")
 		return runResults(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]),
 						  std::atof(argv[7]), argv[8], std::atoi(argv[9]), std::atoi(argv[10]), std::atoi(argv[11]));
+	if (argc >= 8 && std::string(argv[1]) == "tc")
+		return runSteps(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]), 0.0,
+						nullptr, argv[7]);
 	if (argc >= 7 && std::string(argv[1]) == "steps")
 		return runSteps(argv[2], std::atof(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atoi(argv[6]));
 	std::fprintf(stderr, "usage: %s forces <inp> <rc> <rcLJ> <periodic> | lrc <inp> <rc> <rcLJ> | steps <inp> <rc> <rcLJ> <dt> <n> | nvt <inp> <rc> <rcLJ> <dt> <n> <T> | binw <inp> <rc> <prefix> <time> | binr <inp> <header> <data> <rc>\n", argv[0]);
