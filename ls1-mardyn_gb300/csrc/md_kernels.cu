@@ -547,13 +547,14 @@ __global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, con
 }
 
 // Pair-candidate rows of the thread-per-molecule kernels (single-centre LJ)
-// are interleaved in 32-byte blocks (one DRAM sector) across the 32
+// in mixed precision are interleaved in 32-byte blocks (one DRAM sector) across the 32
 // molecules of a warp: block c (entries 8c .. 8c + 7) of molecule i is block
 // ((i / 32) * (maxnb / 8) + c) * 32 + i % 32 of the list, so the lanes of a
 // warp read one kilobyte of consecutive bytes per block instead of one
 // sector from each of 32 rows, and the list build writes whole sectors.
-// The rows of the warp-per-molecule kernels (multi-site) stay row-major
-// (row i at i * maxnb).  maxnb is a multiple of 8.
+// The rows of the warp-per-molecule kernels (multi-site) and of the FP64
+// kernels, which read one entry at a time, stay row-major (row i at
+// i * maxnb).  maxnb is a multiple of 8.
 __device__ __forceinline__ size_t il_block(int64_t i, int c, int maxnb) {
     return ((size_t)(i >> 5) * (size_t)(maxnb >> 3) + (size_t)c) * 32 + (size_t)(i & 31);
 }
@@ -1293,7 +1294,7 @@ __global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __res
         const int h = S.home[i];
         const int cnt = nnb[i];
         for (int k = 0; k < cnt; ++k) {
-            const uint32_t e = __ldg(nbr + il_entry(i, k, maxnb));
+            const uint32_t e = __ldg(nbr + (size_t)i * maxnb + k);  // FP64 mode: row-major rows
             const int j = (int)(e & MD_INDEX_MASK);
             const uint32_t code = e >> MD_CODE_SHIFT;
             double shf[3];
