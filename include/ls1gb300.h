@@ -310,6 +310,10 @@ typedef struct {
 } md_temperature_control;
 int md_set_temperature_control(md_ctx* ctx, const md_temperature_control* tc);
 int md_set_simstep(md_ctx* ctx, int64_t simstep);
+/* md_apply_temperature_control: the temperature control of step `simstep`
+ * for callers that step with the half-step calls (after md_integrate_post,
+ * as Simulation::simulateOneTimestep calls TemperatureControl). */
+int md_apply_temperature_control(md_ctx* ctx, int64_t simstep);
 int md_temperature_control_betas(md_ctx* ctx, int32_t region, double* beta_trans, double* beta_rot);
 
 /* Wait for all work of the context. */

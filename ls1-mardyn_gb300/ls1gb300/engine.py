@@ -74,6 +74,7 @@ def load_library(path: str = LIB_PATH):
     L.md_thermostat_betas.argtypes = [vp, i32, dp, dp]
     L.md_set_temperature_control.argtypes = [vp, C.POINTER(abi.MdTemperatureControl)]
     L.md_set_simstep.argtypes = [vp, i64]
+    L.md_apply_temperature_control.argtypes = [vp, i64]
     L.md_temperature_control_betas.argtypes = [vp, i32, dp, dp]
     L.md_planar_init.argtypes = [vp, C.POINTER(abi.MdPlanarConfig)]
     L.md_planar_apply.argtypes = [vp, dp, dp]
@@ -262,6 +263,10 @@ class Engine:
                 g.ramp_update_start, g.ramp_update_stop = int(ramp["update_start"]), int(ramp["update_stop"])
                 g.ramp_update_freq = int(ramp["update_freq"])
         self._check(self.L.md_set_temperature_control(self.h, C.byref(c)), "md_set_temperature_control")
+
+    def apply_temperature_control(self, step: int):
+        """The temperature control of step ``step`` (after md_integrate_post)."""
+        self._check(self.L.md_apply_temperature_control(self.h, int(step)), "md_apply_temperature_control")
 
     def set_simstep(self, step: int):
         self._check(self.L.md_set_simstep(self.h, int(step)), "md_set_simstep")

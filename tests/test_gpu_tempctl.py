@@ -70,3 +70,31 @@ def test_temperature_control_matches_reference(engine_mod, name):
     assert np.abs(m["v"][o] - g["out_v"]).max() <= 1e-7 * np.abs(g["out_v"]).max()
     if np.abs(g["out_L"]).max() > 0:
         assert np.abs(m["L"][o] - g["out_L"]).max() <= 1e-7 * np.abs(g["out_L"]).max()
+
+
+@pytest.mark.gpu
+def test_temperature_control_step_by_step_equals_run(engine_mod):
+    """md_integrate_pre / md_compute_forces / md_integrate_post with
+    md_apply_temperature_control after each step equal md_run with the
+    temperature control: the same kernels in the same order."""
+    ps, g = golden_io.load("tc_lj500")
+    tc = json.loads(str(g["tc_json"]))
+    a = engine_mod.Engine(ps, g["rc"], g["rc_lj"], precision="fp64", skin=0.3)
+    b = engine_mod.Engine(ps, g["rc"], g["rc_lj"], precision="fp64", skin=0.3)
+    for e in (a, b):
+        e.set_temperature_control(tc)
+        e.forces()
+    dt, n = float(g["dt"]), int(g["nsteps"])
+    rows = []
+    for k in range(1, n + 1):
+        a.pre(dt)
+        fo = a.forces()
+        ko = a.post(dt)
+        a.apply_temperature_control(k)
+        rows.append([fo.upot, fo.virial, ko.summv2])
+    rec = b.run(dt, n)
+    ma, mb = a.molecules(), b.molecules()
+    a.close()
+    b.close()
+    assert np.allclose(np.array(rows), rec[:, :3], rtol=1e-12, atol=0)
+    assert np.array_equal(ma["v"], mb["v"]) and np.array_equal(ma["r"], mb["r"])
