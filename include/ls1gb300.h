@@ -287,10 +287,21 @@ int md_thermostat_betas(md_ctx* ctx, int32_t thermostat, double* beta_trans, dou
  * thermostats inside md_run (Simulation.cpp:1236-1268), applied after each
  * step's global values; md_set_simstep sets the step number of the state
  * (md_run's steps are step + 1, step + 2, ...).  md_temperature_control_betas
- * reads the betas of region r's slabs of the last measurement; the Andersen
- * method of TemperatureControl is not offered. */
+ * reads the betas of region r's slabs of the last measurement.
+ * A region with method MD_TC_ANDERSEN (ControlRegionT::ControlTemperature,
+ * TemperatureControl.cpp:411-419) neither measures nor uses slabs,
+ * directions, exponent or ramp: at each control step every molecule inside
+ * it is selected with probability nu * timestep and gets v_d = g * sqrt(T/m)
+ * and L_d = g' * sqrt(T/m) for d = x, y, z with independent standard normal
+ * g, g' (the reference's shared reserve deviate gives L the translational
+ * deviation too).  The reference draws from one sequential generator in
+ * traversal order; here the draws of molecule `id` at step s in region r
+ * are a counter-based stream keyed by (seed, s, id, r), so a run does not
+ * depend on the order or the number of threads. */
 #define MD_TC_MAX_REGIONS 8
 #define MD_TC_MAX_SLABS 64
+#define MD_TC_VELOCITY_SCALING 0
+#define MD_TC_ANDERSEN 1
 typedef struct {
     double lower[3], upper[3];
     double target_temperature;
@@ -301,12 +312,17 @@ typedef struct {
     int32_t ramp_enabled;
     double ramp_start, ramp_end;
     int64_t ramp_update_start, ramp_update_stop, ramp_update_freq;
+    int32_t method;             /* MD_TC_VELOCITY_SCALING or MD_TC_ANDERSEN    */
+    int32_t reserved;
+    double nu;                  /* Andersen collision frequency                */
 } md_tc_region;
 typedef struct {
     int64_t start, frequency, stop;
     int32_t nregions;
     int32_t reserved;
     md_tc_region regions[MD_TC_MAX_REGIONS];
+    double timestep;            /* integrator time step (Andersen regions)     */
+    uint64_t seed;              /* Andersen draws                              */
 } md_temperature_control;
 int md_set_temperature_control(md_ctx* ctx, const md_temperature_control* tc);
 int md_set_simstep(md_ctx* ctx, int64_t simstep);

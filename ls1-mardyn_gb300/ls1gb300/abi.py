@@ -74,12 +74,13 @@ class MdTcRegion(C.Structure):
                 ("component", C.c_int32), ("numslabs", C.c_int32), ("exponent", C.c_double),
                 ("directions", C.c_int32), ("ramp_enabled", C.c_int32), ("ramp_start", C.c_double),
                 ("ramp_end", C.c_double), ("ramp_update_start", C.c_int64), ("ramp_update_stop", C.c_int64),
-                ("ramp_update_freq", C.c_int64)]
+                ("ramp_update_freq", C.c_int64), ("method", C.c_int32), ("reserved", C.c_int32), ("nu", C.c_double)]
 
 
 class MdTemperatureControl(C.Structure):
     _fields_ = [("start", C.c_int64), ("frequency", C.c_int64), ("stop", C.c_int64), ("nregions", C.c_int32),
-                ("reserved", C.c_int32), ("regions", MdTcRegion * MD_TC_MAX_REGIONS)]
+                ("reserved", C.c_int32), ("regions", MdTcRegion * MD_TC_MAX_REGIONS), ("timestep", C.c_double),
+                ("seed", C.c_uint64)]
 
 
 class MdStepRecord(C.Structure):

@@ -241,20 +241,26 @@ class Engine:
         start, frequency, stop and a list of regions with lower/upper corners (an upper corner None is the
         box length, as the reference's "box"), T, component (1-based, 0 = all), numslabs, exponent,
         directions (bit mask x = 1, y = 2, z = 4) and an optional ramp (start, end, update_start,
-        update_stop, update_freq).  None switches it off."""
+        update_stop, update_freq).  A region with method "andersen" takes nu instead of numslabs, exponent,
+        directions and ramp; ``tc`` then also gives timestep and seed.  None switches it off."""
         if tc is None:
             self._check(self.L.md_set_temperature_control(self.h, None), "md_set_temperature_control")
             return
         c = abi.MdTemperatureControl()
         c.start, c.frequency, c.stop = int(tc["start"]), int(tc["frequency"]), int(tc["stop"])
         c.nregions = len(tc["regions"])
+        c.timestep, c.seed = float(tc.get("timestep", 0.0)), int(tc.get("seed", 8624))
         for k, r in enumerate(tc["regions"]):
             g = c.regions[k]
             for d in range(3):
                 g.lower[d] = float(r["lower"][d])
                 g.upper[d] = float(self.ps.box[d] if r["upper"][d] is None else r["upper"][d])
             g.target_temperature = float(r["T"])
-            g.component, g.numslabs = int(r["component"]), int(r["numslabs"])
+            g.component = int(r["component"])
+            if r.get("method", "velocity_scaling") == "andersen":
+                g.method, g.nu = 1, float(r["nu"])
+                continue
+            g.numslabs = int(r["numslabs"])
             g.exponent, g.directions = float(r["exponent"]), int(r["directions"])
             ramp = r.get("ramp")
             g.ramp_enabled = 1 if ramp else 0

@@ -215,3 +215,51 @@ def read_phasespace_binary(header_text: str, data: bytes):
     out["q"] = a["q"].copy() if "q" in a.dtype.names else np.tile([1.0, 0.0, 0.0, 0.0], (n, 1))
     out["L"] = a["L"].copy() if "L" in a.dtype.names else np.zeros((n, 3))
     return time, box, out
+
+
+# ---------------------------------------------------------------- Andersen
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _mix64(z):
+    """SplitMix64 output function (Steele, Lea and Flood, OOPSLA 2014) on
+    uint64 arrays; arithmetic wraps modulo 2^64."""
+    z = np.asarray(z, np.uint64) + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def andersen_control(ids, comp, r, v, L, masses, region, T, nu_dt, seed, step, index):
+    """One Andersen collision pass of a TemperatureControl region
+    (thermostats/TemperatureControl.cpp:367-379 region and component test,
+    :411-419 the collision), with the counter-based draws the engine uses in
+    place of the reference's sequential generator: draw k of molecule `id`
+    in region `index` at `step` is SplitMix64(key + k) with key =
+    mix(mix(mix(seed ^ mix(step)) ^ id) ^ index); draw 0 < nu_dt selects;
+    draws 1 + 2d, 2 + 2d are a Box-Muller pair, v_d = g sd, L_d = g' sd,
+    sd = sqrt(T / m) (the reference's shared reserve deviate gives L the
+    translational deviation).  ``region``: lower, upper (open box) and the
+    1-based component (0 = all).  Returns new (v, L) and the selection mask."""
+    with np.errstate(over="ignore"):
+        ids = np.asarray(ids, np.uint64)
+        inside = np.ones(len(ids), bool)
+        if region["component"]:
+            inside &= np.asarray(comp) + 1 == region["component"]
+        for d in range(3):
+            inside &= (r[:, d] > region["lower"][d]) & (r[:, d] < region["upper"][d])
+        key = _mix64(np.uint64(seed) ^ _mix64(np.uint64(step)))
+        key = _mix64(_mix64(key ^ ids) ^ np.uint64(index))
+
+        def uniform(k):
+            return (_mix64(key + np.uint64(k)) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+
+        sel = inside & (uniform(0) < nu_dt)
+        sd = np.sqrt(T / np.asarray(masses, float)[np.asarray(comp)])
+        v, L = v.copy(), L.copy()
+        for d in range(3):
+            rad = np.sqrt(-2.0 * np.log(1.0 - uniform(1 + 2 * d)))
+            ang = 2.0 * np.pi * uniform(2 + 2 * d)
+            v[sel, d] = (rad * np.cos(ang) * sd)[sel]
+            L[sel, d] = (rad * np.sin(ang) * sd)[sel]
+    return v, L, sel
