@@ -128,7 +128,8 @@ def test_andersen_apply_matches_oracle(engine_mod, system):
 
 
 @pytest.mark.gpu
-def test_andersen_inside_run(engine_mod):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_andersen_inside_run(engine_mod, precision):
     """md_run with an Andersen region over the whole box that selects every
     molecule (nu dt = 1) beside a velocity-scaling region: after the last
     control step the velocities are the oracle's draws for that step at the
@@ -139,7 +140,7 @@ def test_andersen_inside_run(engine_mod):
     vs = dict(lower=[0.0, 0.0, 0.0], upper=[None, None, None], T=1.0, component=0, numslabs=2, exponent=0.4,
               directions=7)
     reg = _andersen([0.0, 0.0, 0.0], [None, None, None], 2.0, 1.0 / dt)
-    e = engine_mod.Engine(ps, 2.5, precision="fp64", skin=0.3)
+    e = engine_mod.Engine(ps, 2.5, precision=precision, skin=0.3)
     e.set_temperature_control(_tc([vs, reg], dt, seed=5, freq=3))
     e.forces()
     e.run(dt, n)
