@@ -90,6 +90,40 @@ int main(void) {
                        abi.MdBatchConfig.cell_occupancy.offset, abi.MdBatchTuning.trial_occupancy.offset]
 
 
+
+def test_control_struct_layouts_match_header():
+    """Temperature control, planar long-range and kinetic-output structs."""
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "ls1gb300.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(md_tc_region), sizeof(md_temperature_control),
+         offsetof(md_tc_region, ramp_update_freq), offsetof(md_tc_region, method), offsetof(md_tc_region, nu),
+         offsetof(md_temperature_control, regions), offsetof(md_temperature_control, timestep),
+         offsetof(md_temperature_control, seed));
+  printf("%zu %zu %d %d %d %d\n", sizeof(md_planar_config), sizeof(md_kinetic_out), MD_TC_MAX_REGIONS,
+         MD_TC_MAX_SLABS, MD_TC_VELOCITY_SCALING, MD_TC_ANDERSEN);
+  return 0;
+}
+'''
+    d = tempfile.mkdtemp()
+    with open(os.path.join(d, "t.c"), "w") as f:
+        f.write(src)
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), "-o", os.path.join(d, "t"), os.path.join(d, "t.c")],
+                   check=True)
+    out = [int(x) for x in subprocess.run([os.path.join(d, "t")], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    R, T = abi.MdTcRegion, abi.MdTemperatureControl
+    assert out[:8] == [C_size(R), C_size(T), R.ramp_update_freq.offset, R.method.offset, R.nu.offset,
+                       T.regions.offset, T.timestep.offset, T.seed.offset]
+    assert out[8:] == [C_size(abi.MdPlanarConfig), C_size(abi.MdKineticOut), abi.MD_TC_MAX_REGIONS,
+                       abi.MD_TC_MAX_SLABS, 0, 1]
+
+
+def C_size(t):
+    return ctypes.sizeof(t)
+
 def test_batch_create_without_gpu_fails_cleanly(lib):
     import torch
     if torch.cuda.is_available():
