@@ -1,4 +1,5 @@
-"""ctypes binding of the C oracle (test infrastructure only).
+"""ctypes binding of the C oracle, plus the numpy restatement of the
+Andersen regions of TemperatureControl (test infrastructure only).
 
 Used as the checker by tests/, by ``__graft_entry__.smoke()`` and by the CPU
 baseline of ``bench.py``; the engine never imports it.  ``build()`` compiles
