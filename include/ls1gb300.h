@@ -224,7 +224,9 @@ int md_adjoint(md_ctx* ctx, double gU, double gW, const double* gF, double* grad
  * three cells of edge >= rc per axis and at most MD_NOALLOC_MAX_CELLS cells;
  * larger problems return MD_ERR_CAPACITY, too few cells MD_ERR_UNSUPPORTED.
  * The first call on a device (with that device current) looks up the scratch
- * address and should come before any stream capture.  All calls share the
+ * address and should come before any stream capture; so should the first
+ * call after the device was reset or its context replaced, which looks the
+ * address up again (the cache is keyed by the context's id).  All calls share the
  * scratch, which keeps the previous call's contents: calls that overlap on
  * the GPU race and must be serialised by the caller. */
 #define MD_NOALLOC_MAX_N 131072

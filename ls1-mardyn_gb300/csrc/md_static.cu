@@ -21,10 +21,14 @@
 //
 // Set-up: the first call on a device (with that device current) looks up the
 // device address of the array with cudaGetSymbolAddress and caches it for
-// that device; make that first call before any stream capture.
+// that device together with the device's current context; make that first
+// call before any stream capture.  A call that finds another context current
+// (the host program reset the device or replaced its primary context) looks
+// the address up again, so that call too should come before any capture.
 #include <cstdint>
 #include <mutex>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "../../include/ls1gb300.h"
@@ -58,19 +62,60 @@ namespace {
 
 std::mutex g_na_mutex;
 unsigned char* g_na_ptr[NA_MAX_DEVICES] = {nullptr};
+unsigned long long g_na_ctx_id[NA_MAX_DEVICES] = {0};  // context the cached address belongs to
 
-// Device address of the scratch array on the current device (looked up once).
+// The driver's cuCtxGetCurrent and cuCtxGetId, fetched through the runtime
+// (no link-time dependency on libcuda).  A context's id is unique for the
+// life of the process, unlike its handle, which a re-created context may
+// reuse.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+cudaError_t na_driver_fn(const char* name, void** fn) {
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess) return e;
+    return q == cudaDriverEntryPointSuccess && *fn ? cudaSuccess : cudaErrorNotSupported;
+}
+
+// id of the context current on this thread, 0 if there is none
+unsigned long long na_current_ctx_id() {
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array on the current device: looked up on
+// the first call and again whenever the current context is not the one the
+// cached address was taken in (a device reset invalidates the address).
+// cudaGetSymbolAddress also makes the device's primary context current when
+// none is.
 cudaError_t na_scratch_for_device(unsigned char** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= NA_MAX_DEVICES) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev]) {
+    if (!g_ctx_get_current) {
+        void *f1 = nullptr, *f2 = nullptr;
+        if ((e = na_driver_fn("cuCtxGetCurrent", &f1)) != cudaSuccess) return e;
+        if ((e = na_driver_fn("cuCtxGetId", &f2)) != cudaSuccess) return e;
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    }
+    const unsigned long long id = g_na_ptr[dev] ? na_current_ctx_id() : 0;
+    if (!g_na_ptr[dev] || id == 0 || id != g_na_ctx_id[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_md_noalloc_scratch);
         if (e != cudaSuccess) return e;
+        const unsigned long long now = na_current_ctx_id();
+        if (now == 0) return cudaErrorDeviceUninitialized;
         g_na_ptr[dev] = static_cast<unsigned char*>(p);
+        g_na_ctx_id[dev] = now;
     }
     *out = g_na_ptr[dev];
     return cudaSuccess;
@@ -246,13 +291,17 @@ extern "C" int md_forces_lj_noalloc(const double* d_r, int64_t n, const double b
     int64_t ncells = 1;
     for (int d = 0; d < 3; ++d) {
         if (!(box[d] > 0)) return MD_ERR_ARG;
-        g.n[d] = (int)(box[d] / rc);
+        const double q = box[d] / rc;  // cells of edge >= rc along this axis (before truncation)
+        // more cells on one axis than the scratch holds in total (checked before the conversion to int,
+        // which would overflow for a very dilute box)
+        if (!(q < (double)kMaxCells + 1.0)) return MD_ERR_CAPACITY;
+        g.n[d] = (int)q;
         if (g.n[d] < 3) return MD_ERR_UNSUPPORTED;  // needs at least three cells of edge >= rc per axis
         g.L[d] = box[d];
         g.inv[d] = g.n[d] / box[d];
-        ncells *= g.n[d];
+        ncells *= g.n[d];  // <= kMaxCells^2 after any factor: no overflow
+        if (ncells > kMaxCells) return MD_ERR_CAPACITY;  // more cells than the static scratch holds
     }
-    if (ncells > kMaxCells) return MD_ERR_CAPACITY;  // more cells than the static scratch holds
     unsigned char* base = nullptr;
     if (na_scratch_for_device(&base) != cudaSuccess) return MD_ERR_CUDA;
     int* counts = reinterpret_cast<int*>(base + kCountsOff);

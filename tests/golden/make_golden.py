@@ -14,7 +14,7 @@ sources by ``oracle/ref/Makefile`` into ``oracle/_ref/``) on
 and stores inputs and outputs as ``.npz``.  Only this script reads the
 reference tree; the fixtures travel with the repository.
 
-    python tests/golden/make_golden.py --ref /root/reference
+    python tests/golden/make_golden.py [--ref <ls1-mardyn tree>]   (default: oracle/refpath.py)
 """
 import argparse
 import dataclasses
@@ -95,8 +95,12 @@ def jitter(ps, amp, seed):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None)
     a = ap.parse_args()
+    if a.ref is None:
+        sys.path.insert(0, ROOT)
+        from oracle.refpath import reference_tree
+        a.ref = reference_tree()
     tin = os.path.join(a.ref, "test_input")
     tmp = tempfile.mkdtemp()
 

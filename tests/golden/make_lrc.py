@@ -40,8 +40,12 @@ def store(name, ps, rc, rclj, u, w):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None)
     a = ap.parse_args()
+    if a.ref is None:
+        sys.path.insert(0, mg.ROOT)
+        from oracle.refpath import reference_tree
+        a.ref = reference_tree()
     tmp = tempfile.mkdtemp()
     cases = [("lj864", mg.psm.lj_fcc(6, 0.7, 1.1, seed=3), 2.5, 2.5),
              ("lj864_shifted", mg.psm.lj_fcc(6, 0.7, 1.1, seed=3, shifted=True, rc=2.5), 2.5, 2.5),

@@ -12,7 +12,10 @@ import tempfile
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+sys.path.insert(0, ROOT)
+from oracle.refpath import reference_tree  # noqa: E402
+
+REF = reference_tree()
 LS1 = os.path.join(ROOT, "ls1-mardyn_gb300", "ls1")
 OBJ = os.path.join(ROOT, "oracle", "_ref", "obj_DPDP")
 
