@@ -13,13 +13,20 @@ forces, post-force half step and the Upot/virial/kinetic sums.
   e2e     the same metric through the C ABI from host buffers: upload of the
           phase space, the K steps with the per-step sums read back, and the
           download of the final phase space, all inside the timed region;
-  roofline  the pair kernel (dominant kernel): algorithmic bytes per launch /
-          event-timed launch duration against the measured HBM copy
-          bandwidth, with the DRAM traffic scaled from an ncu capture;
-  roofline_fp32  the same launch as the reference's FlopCounter flops per
-          unique in-cutoff pair against the nominal FP32 FMA rate;
+  roofline  the pair kernel (dominant kernel) against the FP32 FMA rate:
+          the reference's FlopCounter flops of the unique in-cutoff pairs per
+          launch / event-timed launch duration, against SMs x 128 lanes x 2
+          flop x the SM clock sampled during the timed region (nominal rate
+          at that clock; the measured-peaks file holds no FP32 figure);
+  roofline_hbm  the same launch as algorithmic bytes against the measured
+          HBM copy bandwidth, with the DRAM traffic scaled from an ncu capture;
+  precision  mixed vs FP64 at the final state of the timed steps: relative rms
+          force error, Upot / virial / pressure errors, pair counts;
+  fp64   the same workload through the FP64 kernel (molecule-updates/s), and
+          the adjoint / forward pair-kernel time ratio;
   cpu_baseline  the CPU oracle (C restatement of the reference's path, OpenMP
-          C08 traversal) on all host cores on a bounded sample of the workload.
+          C08 traversal) on all host cores on the full workload for as many
+          steps as fit in a bounded time.
 
 --impl reference times that CPU path alone (rank 0; other ranks exit 0).
 Multi-GPU: independent replicas (one box per rank, no collective on the data
@@ -64,6 +71,11 @@ BATCH_DESC = ("512 independent periodic 1CLJ boxes, N log-uniform in [500, 20000
               "T* U[0.7, 1.3], rc=2.5, dt=0.002, graphs of 100 steps, skin and threads per molecule row autotuned")
 DEFAULT_SKIN = {"lj4m": 0.25, "lj1m": 0.25, "lj32k": 0.3, "slab": 0.25, "mix1m": 0.1}
 FLOP_PER_PAIR_LJ = 39.0  # reference FlopCounter model: 31 per LJ site pair + 8 per molecule distance
+# FlopCounter flops per unique interacting site pair, by kind (LJ, C-C, C-D, D-D with RF, C-Q, D-Q, Q-Q), and per
+# unique interacting molecule pair for the centre distance (src/utils/FlopCounter.cpp:19-73)
+FLOP_PER_SITE_PAIR = (31.0, 24.0, 52.0, 127.0, 69.0, 141.0, 151.0)
+FLOP_PER_MOL_PAIR = 8.0
+FP32_LANES_PER_SM = 128  # FP32 FMA lanes per SM (4 sub-partitions x 32)
 # DRAM bytes (read + write) of one k_force_lj32x2 launch per pair-candidate list entry, from an ncu
 # capture of the 1,000,188-molecule case (434.2 MB for 100.2 entries per molecule); traffic grows
 # with the entries read, so it is scaled by the live entry count.
@@ -95,6 +107,12 @@ class Cudart:
         self.L.cudaEventSynchronize.argtypes = [C.c_void_p]
         self.L.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
         self.L.cudaEventDestroy.argtypes = [C.c_void_p]
+        self.L.cudaDeviceGetAttribute.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_int]
+
+    def attr(self, which: int, device: int) -> int:
+        v = C.c_int()
+        assert self.L.cudaDeviceGetAttribute(C.byref(v), which, device) == 0
+        return int(v.value)
 
     def event(self):
         e = C.c_void_p()
@@ -165,31 +183,31 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU baseline (oracle)
-def cpu_baseline(workload: str, budget_s: float = 12.0) -> dict:
+def cpu_baseline(workload: str, budget_s: float = 20.0, max_steps: int = 10 ** 9, warmup: int = 0) -> dict:
+    """The oracle (the C restatement of the reference's path: OpenMP C08
+    traversal, scalar loop bodies, Leapfrog) on the full workload with all
+    host cores: a first force pass and `warmup` untimed steps, then NVE steps
+    one at a time until `budget_s` or `max_steps` is reached (at least 2)."""
     from oracle.oracle import Oracle
-    gen, rc, dt, _ = WORKLOADS[workload]
-    if workload in ("lj4m", "lj1m", "slab"):
-        ps = psm.lj_fcc(14, 0.75, 0.9, seed=7)        # 10,976 molecules, same state point
-        sample = "1CLJ fcc 14^3x4 = 10,976 molecules at the same rho*, T*, rc, dt"
-    elif workload == "lj32k":
-        ps = gen()
-        sample = "the full 32,000-molecule box"
-    else:
-        ps = psm.mixture(4000, 18.0, 300.0, seed=7)
-        sample = "2CLJQ/1CLJD mixture, 4,000 molecules, same state point"
+    gen, rc, dt, desc = WORKLOADS[workload]
+    ps = gen()
     threads = os.cpu_count() or 1
     o = Oracle(ps, rc, threads=threads)
     o.rebin()
     o.forces()
+    if warmup:
+        o.run(dt, warmup)
     steps, t0 = 0, time.perf_counter()
     while True:
-        o.run(dt, 5)
-        steps += 5
+        o.run(dt, 1)
+        steps += 1
         el = time.perf_counter() - t0
-        if el > budget_s:
+        if steps >= max_steps or (el > budget_s and steps >= 2):
             break
     return {"value": ps.n * steps / el, "unit": "molecule-updates/s", "cores": threads, "kind": "port",
-            "sample": f"{sample}; {steps} NVE steps in {el:.1f} s with {threads} OpenMP threads"}
+            "molecules": int(ps.n),
+            "sample": f"the full workload ({ps.n:,} molecules); {steps} NVE steps in {el:.1f} s with {threads} "
+                      f"OpenMP threads (oracle: C08 cell pairs, scalar loop bodies, FP64)"}
 
 
 # ---------------------------------------------------------------- main
@@ -244,15 +262,29 @@ def replica_throughput(pg, world: int, n_per_rank: int, steps: int, ms_local: fl
     return world * n_per_rank * steps / (ms * 1e-3), ms
 
 
+def workload_config(a, desc: str, n: int, skin: float) -> dict:
+    """The `config` of the bench line, shared by both arms."""
+    return {"workload": desc, "precision": a.precision, "skin": skin, "molecules": n,
+            "integrator": "LeapfrogRMM (reduced memory mode)" if a.integrator == "rmm" else "Leapfrog",
+            "parallelism": "replicas x1" if a.gpus == 1 else f"replicas x{a.gpus}",
+            "l2": "working set > L2 (GBs), no flush needed"}
+
+
 def run_reference(a, rank):
+    """The reference's CPU path for this workload (the oracle port; the
+    reference tree itself is not on the GPU host) on the full workload, all
+    host cores: min(W, 1) untimed steps, then up to K timed steps within a
+    bounded time."""
     if rank != 0:
         return
-    cb = cpu_baseline(a.workload, budget_s=max(10.0, min(60.0, 0.5 * a.steps)))
     gen, rc, dt, desc = WORKLOADS[a.workload]
+    skin = DEFAULT_SKIN[a.workload] if a.skin is None else a.skin
+    cb = cpu_baseline(a.workload, budget_s=120.0, max_steps=a.steps, warmup=min(a.warmup, 1))
+    n = cb["molecules"]
     line = {"impl": "reference", "metric": "molecule-updates/s", "value": cb["value"], "unit": "molecule-updates/s",
             "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
-            "config": {"workload": desc, "sample": cb["sample"]},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann velocities)",
+            "config": workload_config(a, desc, n, skin),
             "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "molecule-updates/s",
                                         "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -530,10 +562,23 @@ def main():
     value, ms = replica_throughput(pg, world, n, a.steps, ms)
     # per-kernel times on the engine stream, right after the timed region
     fo = eng.forces()
+    mol = eng.molecules()
     kt = eng.time_kernels(5)
+    # precision at the final state of the timed steps: the same positions through the FP64 kernel
+    from ls1gb300 import precision as P
+    prec = None
+    if a.precision == "mixed" and not rmm:
+        prec = P.report(P.state_of(mol, ps), rc, skin=skin, device=local, mixed_forces=(fo, mol))
+    multisite = not (len(ps.components) == 1 and len(ps.components[0].lj) == 1
+                     and not (ps.components[0].charges or ps.components[0].dipoles or ps.components[0].quadrupoles))
     pairs = fo.site_pairs[0]
-    flops = FLOP_PER_PAIR_LJ * pairs
-    fp32_peak = 152 * 128 * 2 * 2070e6 / 1e12   # TFLOP/s at the maximum SM clock
+    if multisite:
+        flops = FLOP_PER_MOL_PAIR * fo.mol_pairs + sum(f * k for f, k in zip(FLOP_PER_SITE_PAIR, fo.site_pairs))
+        flop_desc = (f"FlopCounter model: 8 flop x {fo.mol_pairs} unique interacting molecule pairs + per site-pair "
+                     f"kind (LJ 31, C-C 24, C-D 52, D-D 127, C-Q 69, D-Q 141, Q-Q 151) x {list(fo.site_pairs)}")
+    else:
+        flops = FLOP_PER_PAIR_LJ * pairs
+        flop_desc = f"FlopCounter model: {FLOP_PER_PAIR_LJ:.0f} flop x {pairs} unique in-cutoff LJ pairs per launch"
     list_bytes = kt.mean_candidates * n * 4.0
     # the dominant kernel of the timed steps: in the fused Leapfrog steps the pair kernel that also runs
     # both half steps, else the plain pair kernel
@@ -547,17 +592,57 @@ def main():
                     "coordinates)")
         traffic = STEP_DRAM_BYTES_PER_ENTRY * kt.mean_candidates * n
     else:
-        kname = "k_force_lj32x2" if a.precision == "mixed" else "k_force_lj64"
+        if multisite:
+            kname = "k_force_ms<float>" if a.precision == "mixed" else "k_force_ms<double>"
+        else:
+            kname = "k_force_lj32x2" if a.precision == "mixed" else "k_force_lj64"
         launch_ms = kt.force_ms
         hbm_bytes = list_bytes + n * (16 + 4 + 9 * 8)
         alg_desc = "per launch: 4 B per pair-candidate list entry + 16 B position + 4 B count + 72 B F/M/Vi per molecule"
-        traffic = FORCE_DRAM_BYTES_PER_ENTRY * kt.mean_candidates * n if a.precision == "mixed" else None
+        traffic = (FORCE_DRAM_BYTES_PER_ENTRY * kt.mean_candidates * n
+                   if a.precision == "mixed" and not multisite else None)
     achieved = flops / (launch_ms * 1e-3) / 1e12
+    sms = cu.attr(16, local)                       # cudaDevAttrMultiProcessorCount
+    max_mhz = cu.attr(13, local) / 1e3             # cudaDevAttrClockRate (kHz)
+    sm_mhz = clocks.get("sm_mhz") or max_mhz
+    fp32_peak = sms * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    fp64_lane_note = "FP64 kernel: bound by GB300's FP64 rate, not FP32" if a.precision == "fp64" else None
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     hbm_peak, hbm_src = 6800.0, "fallback"
     if os.path.exists(peaks_path):
         hbm_peak, hbm_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    # adjoint / forward pair-kernel time on this context (1CLJ at full size)
+    adj = {"system": desc, "kernel_forward_ms": kt.force_ms, "kernel_adjoint_ms": kt.adjoint_ms,
+           "adjoint_over_forward": kt.adjoint_ms / kt.force_ms}
     eng.close()
+
+    # ---- the FP64 kernel on the same workload (the engine's own FP64 throughput)
+    fp64 = None
+    if a.precision == "mixed" and not rmm:
+        e64 = E.Engine(ps, rc, precision="fp64", skin=skin, device=local)
+        e64.forces()
+        e64.run(dt, 3, record=False)
+        st64 = e64.stream()
+        c0, c1 = cu.event(), cu.event()
+        k64 = 10
+        cu.record(c0, st64)
+        e64.run(dt, k64, record=False)
+        cu.record(c1, st64)
+        ms64 = cu.elapsed_ms(c0, c1)
+        e64.close()
+        fp64 = {"value": n * k64 / (ms64 * 1e-3), "unit": "molecule-updates/s", "steps": k64,
+                "ms_per_step": ms64 / k64, "mixed_over_fp64": value / (n * k64 / (ms64 * 1e-3))}
+    # the adjoint on the differentiation workload's mixture (2CLJQ/1CLJD, ~100,000 molecules)
+    adj_mix = None
+    if a.workload == "lj4m" and a.precision == "mixed" and not rmm:
+        mps = psm.mixture(100_000, 18.0, 300.0, seed=4)
+        em = E.Engine(mps, 1.0, precision="mixed", skin=0.1, device=local)
+        em.forces()
+        ktm = em.time_kernels(5)
+        em.close()
+        adj_mix = {"system": f"2CLJQ/1CLJD mixture, {mps.n:,} molecules, n=18 nm^-3, T=300 K, rc=1 nm",
+                   "kernel_forward_ms": ktm.force_ms, "kernel_adjoint_ms": ktm.adjoint_ms,
+                   "adjoint_over_forward": ktm.adjoint_ms / ktm.force_ms}
 
     # ---- end to end through the C ABI with host buffers
     e2e = None
@@ -578,6 +663,8 @@ def main():
                   "download_s": t1 - t_run}
         h2d = sum(x.nbytes for x in (ids, comp, r, v, q, Lm))
         d2h = sum(out[k].nbytes for k in out) + rec.nbytes
+        phases["upload_gbs"] = h2d / phases["create_upload_s"] / 1e9
+        phases["download_gbs"] = sum(out[k].nbytes for k in out) / phases["download_s"] / 1e9
         e2e = {"value": world * n * a.steps / e2e_s, "unit": "molecule-updates/s",
                "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps,
                "scope": "md_create + upload + first forces + K steps (per-step sums read back) + download",
@@ -586,6 +673,7 @@ def main():
     cb = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         cb = cpu_baseline(a.workload)
+        cb.pop("molecules", None)
 
     if rank == 0:
         line = {
@@ -593,9 +681,7 @@ def main():
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-pairs/f64-state" if a.precision == "mixed" else "f64",
             "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann velocities)",
-            "config": {"workload": desc, "precision": a.precision, "skin": skin, "molecules": n,
-                       "integrator": "LeapfrogRMM (reduced memory mode)" if rmm else "Leapfrog",
-                       "parallelism": f"replicas x{world}", "l2": "working set > L2 (GBs), no flush needed"},
+            "config": workload_config(a, desc, n, skin),
             # graph-captured chunks of 25 steps: the per-step kernels, the rebuild kernels of the steps that
             # rebuilt the list, and per chunk the half steps that are not fused (mixed single-centre LJ: the
             # first pre-force and the last post-force half step; otherwise the first pre-force one); the reduced
@@ -605,20 +691,28 @@ def main():
                                 + kt.launches_per_rebuild * rebuilds_timed
                                 + ((1 if a.precision == "mixed" else 0) if rmm else (2 if fused else 1))
                                 * -(-a.steps // 25)),
-            "roofline": {"bound": "hbm", "kernel": kname,
-                         "achieved": hbm_bytes / (launch_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": hbm_bytes / (launch_ms * 1e-3) / 1e9 / hbm_peak,
-                         "traffic": traffic, "peak_source": hbm_src,
-                         "algorithmic": alg_desc, "algorithmic_bytes": hbm_bytes, "launch_ms": launch_ms},
-            "roofline_fp32": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                              "frac": achieved / fp32_peak,
-                              "algorithmic": f"{FLOP_PER_PAIR_LJ:.0f} flop x {pairs} unique in-cutoff pairs per launch",
-                              "peak_source": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 flop x 2070 MHz"},
+            "roofline": {"bound": "fp32", "kernel": kname, "achieved": achieved, "peak": fp32_peak,
+                         "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
+                         "peak_source": (f"nominal FP32 FMA rate at the sampled SM clock: {sms} SMs (device) x "
+                                         f"{FP32_LANES_PER_SM} lanes x 2 flop x {sm_mhz:.0f} MHz"),
+                         "algorithmic": flop_desc, "algorithmic_flops": flops, "launch_ms": launch_ms,
+                         "note": fp64_lane_note},
+            "roofline_hbm": {"bound": "hbm", "kernel": kname,
+                             "achieved": hbm_bytes / (launch_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": hbm_bytes / (launch_ms * 1e-3) / 1e9 / hbm_peak,
+                             "traffic": traffic, "peak_source": hbm_src,
+                             "algorithmic": alg_desc, "algorithmic_bytes": hbm_bytes, "launch_ms": launch_ms},
+            "precision": prec,
+            "fp64": fp64,
+            "adjoint": {"lj": adj, "mixture": adj_mix,
+                        "value": max(x["adjoint_over_forward"] for x in (adj, adj_mix) if x),
+                        "unit": "adjoint / forward pair-kernel time"},
             "kernels_ms": {"force": kt.force_ms, "force_with_both_half_steps": kt.step_force_ms, "pre": kt.pre_ms,
                            "post": kt.post_ms, "rebuild": kt.rebuild_ms},
             "pair_list": {"mean_candidates": kt.mean_candidates, "rebuilds": int(kt.rebuilds),
                           "rebuilds_timed": int(rebuilds_timed)},
-            "physics": {"upot_per_molecule": fo.upot / n, "unique_lj_pairs": int(pairs)},
+            "physics": {"upot_per_molecule": fo.upot / n, "unique_lj_pairs": int(pairs),
+                        "unique_molecule_pairs": int(fo.mol_pairs)},
             "clocks": clocks,
             "e2e": e2e,
             "cpu_baseline": cb,
