@@ -222,6 +222,9 @@ def parse():
     ap.add_argument("--skin", type=float, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--pair-scheme", default="rows", choices=["rows", "newton3"],
+                    help="rows: per-molecule candidate rows, each pair from both sides; newton3: every pair once "
+                         "(Newton-3 cluster pairs) where the system allows")
     ap.add_argument("--integrator", default="leapfrog", choices=["leapfrog", "rmm"],
                     help="rmm: the reduced memory mode (LeapfrogRMM + VCP1CLJRMM, 1CLJ only)")
     return ap.parse_args()
@@ -543,7 +546,7 @@ def main():
     def steps(e, k, record):
         return e.rmm_run(dt, k, record=record) if rmm else e.run(dt, k, record=record)
 
-    eng = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local)
+    eng = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local, pair_scheme=a.pair_scheme)
     fo0 = first_forces(eng)
     steps(eng, max(3, a.warmup), False)
     eng.sync()
@@ -582,8 +585,17 @@ def main():
     list_bytes = kt.mean_candidates * n * 4.0
     # the dominant kernel of the timed steps: in the fused Leapfrog steps the pair kernel that also runs
     # both half steps, else the plain pair kernel
-    step_kernel = fused and not rmm and kt.step_force_ms > 0
-    if step_kernel:
+    n3 = kt.pair_scheme == 1
+    step_kernel = fused and not rmm and kt.step_force_ms > 0 and not n3
+    if n3:
+        kname = f"k_force_n3 (Newton-3 cluster pairs, {kt.cluster_size} molecules per cluster)"
+        launch_ms = kt.force_ms
+        ncl = n / kt.cluster_size
+        hbm_bytes = list_bytes + n * (16 + 32) + ncl * 12
+        alg_desc = ("per launch: 4 B per cluster-list entry + 16 B position + 32 B force accumulator (read and "
+                    "written) per molecule + 12 B cluster record and list length per cluster")
+        traffic = None
+    elif step_kernel:
         kname = "k_force_lj32x2<EPI_LEAPFROG> (pair kernel with both Leapfrog half steps)"
         launch_ms = kt.step_force_ms
         hbm_bytes = list_bytes + n * STEP_BYTES_PER_MOLECULE
@@ -632,6 +644,29 @@ def main():
         e64.close()
         fp64 = {"value": n * k64 / (ms64 * 1e-3), "unit": "molecule-updates/s", "steps": k64,
                 "ms_per_step": ms64 / k64, "mixed_over_fp64": value / (n * k64 / (ms64 * 1e-3))}
+    # the Newton-3 cluster-pair path on the same workload (every pair evaluated once), device-timed like `value`
+    newton3 = None
+    if fused and not rmm and a.pair_scheme == "rows":
+        e3 = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local, pair_scheme="newton3")
+        e3.forces()
+        e3.run(dt, max(3, a.warmup), record=False)
+        st3 = e3.stream()
+        c0, c1 = cu.event(), cu.event()
+        rb3 = e3.rebuilds()
+        cu.record(c0, st3)
+        e3.run(dt, a.steps, record=False)
+        cu.record(c1, st3)
+        ms3 = cu.elapsed_ms(c0, c1)
+        rb3 = e3.rebuilds() - rb3
+        f3 = e3.forces()
+        kt3 = e3.time_kernels(5)
+        e3.close()
+        a3 = FLOP_PER_PAIR_LJ * f3.site_pairs[0] / (kt3.force_ms * 1e-3) / 1e12
+        newton3 = {"value": n * a.steps / (ms3 * 1e-3), "unit": "molecule-updates/s", "ms_per_step": ms3 / a.steps,
+                   "kernel": f"k_force_n3 ({kt3.cluster_size} molecules per cluster) + k_n3_lf (both half steps)",
+                   "pair_kernel_ms": kt3.force_ms, "half_steps_ms": kt3.lf_ms, "rebuild_ms": kt3.rebuild_ms,
+                   "rebuilds_timed": int(rb3), "list_entries_per_molecule": kt3.mean_candidates,
+                   "pair_kernel_tflops": a3, "pair_kernel_frac_fp32": a3 / fp32_peak}
     # the adjoint on the differentiation workload's mixture (2CLJQ/1CLJD, ~100,000 molecules)
     adj_mix = None
     if a.workload == "lj4m" and a.precision == "mixed" and not rmm:
@@ -649,7 +684,7 @@ def main():
     if not a.no_e2e:
         ids, comp, r, v, q, Lm = E.abi.molecule_arrays(ps)
         t0 = time.perf_counter()
-        eng2 = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local)
+        eng2 = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local, pair_scheme=a.pair_scheme)
         t_up = time.perf_counter()
         first_forces(eng2)
         t_f = time.perf_counter()
@@ -704,12 +739,15 @@ def main():
                              "algorithmic": alg_desc, "algorithmic_bytes": hbm_bytes, "launch_ms": launch_ms},
             "precision": prec,
             "fp64": fp64,
+            "newton3": newton3,
             "adjoint": {"lj": adj, "mixture": adj_mix,
                         "value": max(x["adjoint_over_forward"] for x in (adj, adj_mix) if x),
                         "unit": "adjoint / forward pair-kernel time"},
-            "kernels_ms": {"force": kt.force_ms, "force_with_both_half_steps": kt.step_force_ms, "pre": kt.pre_ms,
-                           "post": kt.post_ms, "rebuild": kt.rebuild_ms},
-            "pair_list": {"mean_candidates": kt.mean_candidates, "rebuilds": int(kt.rebuilds),
+            "kernels_ms": {"force": kt.force_ms, "force_with_both_half_steps": kt.step_force_ms,
+                           "half_steps_after_pairs": kt.lf_ms, "pre": kt.pre_ms, "post": kt.post_ms,
+                           "rebuild": kt.rebuild_ms},
+            "pair_list": {"scheme": "cluster pairs (every pair once)" if n3 else "per-molecule rows",
+                          "entries_per_molecule": kt.mean_candidates, "rebuilds": int(kt.rebuilds),
                           "rebuilds_timed": int(rebuilds_timed)},
             "physics": {"upot_per_molecule": fo.upot / n, "unique_lj_pairs": int(pairs),
                         "unique_molecule_pairs": int(fo.mol_pairs)},

@@ -81,8 +81,17 @@ typedef struct {
     int64_t capacity;   /* molecules to reserve (0: size from the first upload)           */
     double skin;        /* Verlet skin of the pair-candidate list; 0 rebuilds every step  */
     int32_t device;     /* CUDA device ordinal                                            */
-    int32_t reserved;
+    int32_t pair_scheme;/* MD_PAIRS_ROWS (0): per-molecule candidate rows, each pair
+                           evaluated from both sides; MD_PAIRS_NEWTON3 (1): every pair
+                           evaluated once (Newton's third law, as
+                           VectorizedCellProcessor::processCellPair, VCP.cpp:2744-2819) by
+                           cluster pairs where the system allows (one component of
+                           single-centre LJ molecules, mixed precision, rc_lj = rc, at least
+                           three list cells per periodic dimension), rows elsewhere         */
 } md_config;
+
+#define MD_PAIRS_ROWS 0
+#define MD_PAIRS_NEWTON3 1
 
 /* One component (molecule type).  Site tables are row-major doubles:
  *   lj:         n_lj x 7         x y z m eps sigma shift6
@@ -377,9 +386,15 @@ typedef struct {
     int32_t launches_per_rebuild; /* kernels a list rebuild adds to such a step         */
     double adjoint_ms;        /* one md_adjoint kernel pass (gU = gW = 1, no gF),
                                  without its host copies                                */
-    double step_force_ms;     /* one pair kernel with both Leapfrog half steps fused, as
-                                 md_run runs it for one component of single-centre LJ
-                                 molecules in mixed precision; 0 otherwise              */
+    double step_force_ms;     /* the pair evaluation of one md_run step of one component of
+                                 single-centre LJ molecules in mixed precision with both
+                                 Leapfrog half steps: the pair kernel with the half steps
+                                 fused (rows), or the Newton-3 pair kernel plus its
+                                 half-step kernel (cluster pairs); 0 otherwise          */
+    double lf_ms;             /* cluster pairs: that half-step kernel alone; 0 otherwise */
+    int32_t pair_scheme;      /* the scheme the context's pair evaluations use now:
+                                 MD_PAIRS_NEWTON3 (cluster pairs) or MD_PAIRS_ROWS       */
+    int32_t cluster_size;     /* molecules per cluster of the Newton-3 path             */
 } md_kernel_times;
 
 int md_get_stream(md_ctx* ctx, void** stream);

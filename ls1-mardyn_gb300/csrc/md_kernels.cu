@@ -367,8 +367,11 @@ __device__ void wrap_molecule(State& S, int64_t i, unsigned* status, unsigned lo
 
 // Leaving-particle wrap for molecules outside the box, then the list cell of
 // every molecule and its histogram.
+// With msub (the Newton-3 cluster path) also the octant of the list cell the
+// molecule lies in, in Morton order (x bit 0, y bit 1, z bit 2), for the
+// order inside the cell.
 __global__ void k_list_hist(State S, int* mcell, int* counts, unsigned* status, unsigned long long* nwrapped,
-                            const unsigned* need) {
+                            const unsigned* need, unsigned char* msub) {
     if (!*need) return;
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= S.n) return;
@@ -379,6 +382,14 @@ __global__ void k_list_hist(State S, int* mcell, int* counts, unsigned* status, 
     int c = (cz * cP.ln[1] + cy) * cP.ln[0] + cx;
     mcell[i] = c;
     atomicAdd(&counts[c], 1);
+    if (msub) {
+        const int o[3] = {cx, cy, cz};
+        const double r[3] = {S.rx[i], S.ry[i], S.rz[i]};
+        unsigned char k = 0;
+        for (int d = 0; d < 3; ++d)
+            if ((r[d] - cP.bmin[d]) * cP.linv[d] - o[d] >= 0.5) k |= (unsigned char)(1u << d);
+        msub[i] = k;
+    }
 }
 
 // Exclusive scan of counts[0..n) into start[0..n] (and cursor) in three
@@ -466,11 +477,14 @@ __global__ void k_list_scatter(int64_t n, const int* mcell, int* cursor, int* pe
 // the pair kernels see runs of one component), then by previous slot.  Cells
 // of up to 64 molecules are ranked in registers; larger cells fall back to a
 // serial insertion sort by lane 0.
-__device__ __forceinline__ int cell_sort_key(const int* comp, int v) {
-    return comp ? (comp[v] << MD_CODE_SHIFT) | v : v;
+// With msub (one component, the Newton-3 cluster path) by octant of the cell
+// first, so that runs of consecutive slots are compact clusters.
+__device__ __forceinline__ int cell_sort_key(const int* comp, const unsigned char* msub, int v) {
+    return comp ? (comp[v] << MD_CODE_SHIFT) | v : (msub ? ((int)msub[v] << MD_CODE_SHIFT) | v : v);
 }
 
-__global__ void k_cell_sort(const int* start, int ncells, int* perm, const int* comp, const unsigned* need) {
+__global__ void k_cell_sort(const int* start, int ncells, int* perm, const int* comp, const unsigned* need,
+                            const unsigned char* msub) {
     if (!*need) return;
     int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -478,8 +492,8 @@ __global__ void k_cell_sort(const int* start, int ncells, int* perm, const int* 
     int b = start[c], e = start[c + 1], m = e - b;
     if (m <= 1) return;
     if (m <= 64) {
-        int v0 = lane < m ? cell_sort_key(comp, perm[b + lane]) : 0x7fffffff;
-        int v1 = lane + 32 < m ? cell_sort_key(comp, perm[b + lane + 32]) : 0x7fffffff;
+        int v0 = lane < m ? cell_sort_key(comp, msub, perm[b + lane]) : 0x7fffffff;
+        int v1 = lane + 32 < m ? cell_sort_key(comp, msub, perm[b + lane + 32]) : 0x7fffffff;
         int r0 = 0, r1 = 0;
         for (int t = 0; t < 32; ++t) {
             int a0 = __shfl_sync(0xffffffffu, v0, t), a1 = __shfl_sync(0xffffffffu, v1, t);
@@ -493,9 +507,9 @@ __global__ void k_cell_sort(const int* start, int ncells, int* perm, const int* 
     }
     if (lane == 0) {
         for (int k = b + 1; k < e; ++k) {
-            const int v = perm[k], kv = cell_sort_key(comp, v);
+            const int v = perm[k], kv = cell_sort_key(comp, msub, v);
             int q = k - 1;
-            while (q >= b && cell_sort_key(comp, perm[q]) > kv) { perm[q + 1] = perm[q]; --q; }
+            while (q >= b && cell_sort_key(comp, msub, perm[q]) > kv) { perm[q + 1] = perm[q]; --q; }
             perm[q + 1] = v;
         }
     }
@@ -1872,6 +1886,7 @@ __global__ void k_post_pre(State S, Kick K, double* partials, int pstride, float
     }
 }
 
+#include "md_n3.inc"
 #include "md_adjoint.inc"
 #include "md_api.inc"
 #include "md_planar.inc"

@@ -34,7 +34,7 @@ class MdConfig(C.Structure):
     _fields_ = [("box_min", C.c_double * 3), ("box_max", C.c_double * 3), ("rc", C.c_double),
                 ("rc_lj", C.c_double), ("eps_rf", C.c_double), ("periodic", C.c_int32 * 3),
                 ("precision", C.c_int32), ("capacity", C.c_int64), ("skin", C.c_double),
-                ("device", C.c_int32), ("reserved", C.c_int32)]
+                ("device", C.c_int32), ("pair_scheme", C.c_int32)]
 
 
 class MdComponent(C.Structure):
@@ -91,7 +91,8 @@ class MdKernelTimes(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("pre_ms", C.c_double), ("post_ms", C.c_double),
                 ("rebuild_ms", C.c_double), ("mean_candidates", C.c_double), ("rebuilds", C.c_int64),
                 ("launches_per_step", C.c_int32), ("launches_per_rebuild", C.c_int32),
-                ("adjoint_ms", C.c_double), ("step_force_ms", C.c_double)]
+                ("adjoint_ms", C.c_double), ("step_force_ms", C.c_double), ("lf_ms", C.c_double),
+                ("pair_scheme", C.c_int32), ("cluster_size", C.c_int32)]
 
 
 class MdBatchConfig(C.Structure):
@@ -121,7 +122,7 @@ def dptr(a: np.ndarray):
 
 def make_config(box, rc: float, rc_lj: float, eps_rf: float, periodic: Sequence[int] = (1, 1, 1),
                 precision: int = MD_PREC_FP64, capacity: int = 0, skin: float = 0.0, device: int = 0,
-                box_min=(0.0, 0.0, 0.0)) -> MdConfig:
+                box_min=(0.0, 0.0, 0.0), pair_scheme: int = 0) -> MdConfig:
     cfg = MdConfig()
     for d in range(3):
         cfg.box_min[d] = float(box_min[d])
@@ -129,6 +130,7 @@ def make_config(box, rc: float, rc_lj: float, eps_rf: float, periodic: Sequence[
         cfg.periodic[d] = int(periodic[d])
     cfg.rc, cfg.rc_lj, cfg.eps_rf = float(rc), float(rc_lj), float(eps_rf)
     cfg.precision, cfg.capacity, cfg.skin, cfg.device = int(precision), int(capacity), float(skin), int(device)
+    cfg.pair_scheme = int(pair_scheme)
     return cfg
 
 

@@ -28,6 +28,7 @@ HEADER = os.path.join(os.path.dirname(PKG), "include", "ls1gb300.h")
 _lib = None
 
 PRECISION = {"fp64": abi.MD_PREC_FP64, "mixed": abi.MD_PREC_MIXED}
+PAIR_SCHEME = {"rows": 0, "newton3": 1}
 
 
 class EngineError(RuntimeError):
@@ -100,11 +101,15 @@ class Engine:
 
     def __init__(self, ps: PhaseSpace, rc: float, rc_lj: Optional[float] = None,
                  periodic: Sequence[int] = (1, 1, 1), precision: str = "fp64", skin: float = 0.0,
-                 device: int = 0, capacity: int = 0):
+                 device: int = 0, capacity: int = 0, pair_scheme: str = "rows"):
+        """pair_scheme "rows": per-molecule candidate rows, each pair evaluated from both sides;
+        "newton3": every pair evaluated once (Newton's third law, cluster pairs) where the system allows
+        it (one component of single-centre LJ molecules, mixed precision), rows elsewhere."""
         self.L = load_library()
         self.ps = ps
         self.cfg = abi.make_config(ps.box, rc, rc if rc_lj is None else rc_lj, ps.eps_rf, periodic,
-                                   PRECISION[precision], capacity, skin, device)
+                                   PRECISION[precision], capacity, skin, device,
+                                   pair_scheme=PAIR_SCHEME[pair_scheme])
         self.h = C.c_void_p()
         self._check(self.L.md_create(C.byref(self.h), C.byref(self.cfg)), "md_create")
         self.tables = abi.ComponentTables(ps.components, ps.mixing)

@@ -93,6 +93,30 @@ def test_precision_and_pair_counts_at_full_size(mods, name):
     assert abs(fo6.virial - foo.virial) <= 1e-10 * abs(foo.virial)
 
 
+@pytest.mark.parametrize("name", ["C2a_lj4m", "C2b_slab3m"])
+def test_newton3_at_full_size(mods, name):
+    """The Newton-3 cluster-pair path at the 1CLJ benchmark sizes: the same
+    interacting pair counts as the FP64 kernel (exact), relative rms force
+    error <= 1e-5 and Upot, virial <= 1e-6 against it."""
+    E, psm, P = mods
+    gen, rc, dt, skin, nsteps = CONFIGS[name]
+    ps0 = gen(psm)
+    e = E.Engine(ps0, rc, precision="mixed", skin=skin, pair_scheme="newton3")
+    e.forces()
+    e.run(dt, nsteps, record=False)
+    assert e.time_kernels(1).pair_scheme == 1
+    ps = P.state_of(e.molecules(), ps0)
+    fom = e.forces()
+    mm = e.molecules()
+    e.close()
+    rep = P.report(ps, rc, skin=skin, mixed_forces=(fom, mm))
+    print(name, "newton3", rep)
+    assert rep["pairs_equal"], rep
+    assert rep["force_rel_rms"] <= 1e-5, rep
+    for k in ("upot_rel", "virial_rel", "pressure_rel"):
+        assert rep[k] <= 1e-6, rep
+
+
 def _drift(En):
     return abs(En[-1000:].mean() - En[100:1100].mean()) / abs(En[0])
 

@@ -121,6 +121,23 @@ def test_nve_matches_reference(engine_mod, name, precision):
             assert np.abs(m[key][a] - g[gk][b]).max() < 1e-7, key
 
 
+@pytest.mark.parametrize("name", NVE_CASES)
+def test_newton3_nve_matches_reference(engine_mod, name):
+    """The Newton-3 cluster-pair path (mixed precision, every pair once) over
+    the reference's NVE runs, to the mixed tolerance (1e-4 on the per-step
+    sums), where the box allows it (one component of single-centre LJ
+    molecules, three list cells per axis); other cases use the rows."""
+    ps, g = golden_io.load(name)
+    e = engine_mod.Engine(ps, g["rc"], g["rc_lj"], (1, 1, 1), precision="mixed", skin=0.3 * g["rc"],
+                          pair_scheme="newton3")
+    e.forces()
+    rec = e.run(float(g["dt"]), int(g["nsteps"]))
+    ref = g["steps"][1:, 1:]
+    for col in range(4):
+        scale = max(np.abs(ref[:, col]).max(), 1e-300)
+        assert np.abs(rec[:, col] - ref[:, col]).max() <= 1e-4 * scale, col
+
+
 def test_skin_does_not_change_the_trajectory(engine_mod):
     """The pair-candidate list with a skin finds exactly the pairs of the
     rebuild-every-step schedule: FP64 runs with skin 0 and skin 0.4 agree."""
@@ -152,18 +169,24 @@ def test_step_by_step_equals_md_run(engine_mod):
     assert np.allclose(np.array(manual), rec[:, :3], rtol=1e-12, atol=0)
 
 
-def test_fused_leapfrog_steps_equal_step_by_step(engine_mod):
+@pytest.mark.parametrize("scheme", ["rows", "newton3"])
+def test_fused_leapfrog_steps_equal_step_by_step(engine_mod, scheme):
     """Mixed precision, one component of single-centre LJ molecules: md_run
-    fuses the post-force half step of each step and the pre-force half step
-    of the next into the pair kernel (two position buffers).  60 steps (two
-    graph-captured chunks and an eager remainder, several list rebuilds)
-    against md_integrate_pre / md_compute_forces / md_integrate_post: the same
+    runs Leapfrog's post-force half step of each step and the pre-force half
+    step of the next with the pair evaluation -- in the row kernel's epilogue
+    (two position buffers) with per-molecule rows, in k_n3_lf after the
+    Newton-3 pair kernel with cluster pairs.  60 steps (two graph-captured
+    chunks and an eager remainder, several list rebuilds) against
+    md_integrate_pre / md_compute_forces / md_integrate_post.  Rows: the same
     FP64 operations, so positions, velocities, Upot and virial agree bit for
-    bit; the kinetic sums are FP32 products in the fused kernel (1e-6)."""
+    bit, the kinetic sums (FP32 products in the fused kernel) to 1e-6.
+    Cluster pairs: the force accumulators take their atomic additions in an
+    arbitrary order, so both runs agree to FP32 rounding carried over 60
+    steps: Upot, virial and kinetic sums to 1e-5, positions to 1e-5."""
     ps, g = golden_io.load("per_lj500")
     rng = np.random.default_rng(5)
     ps.v = ps.v * 1.5 + rng.normal(0.0, 0.2, ps.v.shape)
-    cells = engine_mod.GpuLinkedCells(ps, 2.5, precision="mixed", skin=0.2)
+    cells = engine_mod.GpuLinkedCells(ps, 2.5, precision="mixed", skin=0.2, pair_scheme=scheme)
     lf = engine_mod.GpuLeapfrog(0.004)
     cells.traverseCells()
     manual = []
@@ -173,16 +196,63 @@ def test_fused_leapfrog_steps_equal_step_by_step(engine_mod):
         ko = lf.eventForcesCalculated(cells)
         manual.append([fo.upot, fo.virial, ko.summv2])
     manual = np.array(manual)
-    e = engine_mod.Engine(ps, 2.5, precision="mixed", skin=0.2)
+    e = engine_mod.Engine(ps, 2.5, precision="mixed", skin=0.2, pair_scheme=scheme)
     e.forces()
     rec = e.run(0.004, 60)
     a, b = cells.molecules(), e.molecules()
     assert e.rebuilds() >= 3
+    assert e.time_kernels(1).pair_scheme == (1 if scheme == "newton3" else 0)
     e.close()
-    np.testing.assert_array_equal(rec[:, :2], manual[:, :2])
-    assert np.abs(rec[:, 2] - manual[:, 2]).max() <= 1e-6 * np.abs(manual[:, 2]).max()
-    for k in ("ids", "r", "v", "F"):
-        np.testing.assert_array_equal(a[k], b[k])
+    if scheme == "rows":
+        np.testing.assert_array_equal(rec[:, :2], manual[:, :2])
+        assert np.abs(rec[:, 2] - manual[:, 2]).max() <= 1e-6 * np.abs(manual[:, 2]).max()
+        for k in ("ids", "r", "v", "F"):
+            np.testing.assert_array_equal(a[k], b[k])
+        return
+    for col in range(3):
+        assert np.abs(rec[:, col] - manual[:, col]).max() <= 1e-5 * np.abs(manual[:, col]).max(), col
+    ia, ib = _by_id(a["ids"]), _by_id(b["ids"])
+    assert np.abs(a["r"][ia] - b["r"][ib]).max() <= 1e-5
+
+
+@pytest.mark.parametrize("name", ["per_lj4000j", "nve_lj32000", "per_lj500"])
+def test_cluster_pairs_match_candidate_rows(engine_mod, name):
+    """Mixed precision: the Newton-3 cluster-pair path (every pair once) and
+    the per-molecule candidate rows (every pair from both sides) on the same
+    state: interacting pair counts equal, forces and per-molecule virials to
+    1e-6 relative rms, Upot and virial to 1e-6 relative; and boxes with fewer
+    than three list cells along a periodic axis fall back to the rows."""
+    ps, g = golden_io.load(name)
+    rng = np.random.default_rng(11)
+    ps.r = ps.r + rng.uniform(-0.05, 0.05, ps.r.shape)
+    out = {}
+    for scheme in ("newton3", "rows"):
+        e = engine_mod.Engine(ps, g["rc"], g["rc_lj"], precision="mixed", skin=0.25, pair_scheme=scheme)
+        fo = e.forces()
+        m = e.molecules()
+        out[scheme] = (fo, m, e.time_kernels(1).pair_scheme)
+        e.close()
+    assert out["newton3"][2] == 1 and out["rows"][2] == 0
+    fa, ma, _ = out["newton3"]
+    fr, mr, _ = out["rows"]
+    assert fa.mol_pairs == fr.mol_pairs and list(fa.site_pairs) == list(fr.site_pairs)
+    ia, ir = _by_id(ma["ids"]), _by_id(mr["ids"])
+    assert _rel_rms(ma["F"][ia], mr["F"][ir]) <= 1e-6
+    assert _rel_rms(ma["Vi"][ia], mr["Vi"][ir]) <= 1e-6
+    assert np.all(ma["M"] == 0.0)
+    assert abs(fa.upot - fr.upot) <= 1e-6 * abs(fr.upot)
+    assert abs(fa.virial - fr.virial) <= 1e-6 * abs(fr.virial)
+    # a box of 2 x 2 x 2 list cells: rows
+    small = psm_small()
+    e = engine_mod.Engine(small, 2.5, precision="mixed", skin=0.25, pair_scheme="newton3")
+    e.forces()
+    assert e.time_kernels(1).pair_scheme == 0
+    e.close()
+
+
+def psm_small():
+    from ls1gb300 import phasespace as psm
+    return psm.lj_fcc(4, 0.8, 1.0, seed=3)   # L = 6.84: two list cells of edge >= 2.75 per axis
 
 
 def test_mixed_matches_fp64_at_scale(engine_mod):
