@@ -682,15 +682,23 @@ def main():
     # ---- end to end through the C ABI with host buffers
     e2e = None
     if not a.no_e2e:
-        ids, comp, r, v, q, Lm = E.abi.molecule_arrays(ps)
+        # the caller's buffers: page-locked input arrays and output arrays, made before the timed region
+        from ls1gb300 import pinned
+        host_in = tuple(pinned.copy(x) for x in E.abi.molecule_arrays(ps))
+        ids, comp, r, v, q, Lm = host_in
+        host_out = {k: pinned.empty(shp, dt) for k, shp, dt in
+                    (("ids", (n,), np.uint64), ("comp", (n,), np.int32), ("r", (n, 3), np.float64),
+                     ("v", (n, 3), np.float64), ("q", (n, 4), np.float64), ("L", (n, 3), np.float64),
+                     ("F", (n, 3), np.float64), ("M", (n, 3), np.float64), ("Vi", (n, 3), np.float64))}
         t0 = time.perf_counter()
-        eng2 = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local, pair_scheme=a.pair_scheme)
+        eng2 = E.Engine(ps, rc, precision=a.precision, skin=skin, device=local, pair_scheme=a.pair_scheme,
+                        arrays=host_in)
         t_up = time.perf_counter()
         first_forces(eng2)
         t_f = time.perf_counter()
         rec = steps(eng2, a.steps, True)
         t_run = time.perf_counter()
-        out = eng2.molecules()
+        out = eng2.molecules(host_out)
         t1 = time.perf_counter()
         e2e_s = max_over_ranks(pg, t1 - t0)
         eng2.close()
@@ -702,7 +710,8 @@ def main():
         phases["download_gbs"] = sum(out[k].nbytes for k in out) / phases["download_s"] / 1e9
         e2e = {"value": world * n * a.steps / e2e_s, "unit": "molecule-updates/s",
                "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps,
-               "scope": "md_create + upload + first forces + K steps (per-step sums read back) + download",
+               "scope": "md_create + upload + first forces + K steps (per-step sums read back) + download, from "
+                        "and into the caller's page-locked host arrays",
                "phases": phases}
 
     cb = None

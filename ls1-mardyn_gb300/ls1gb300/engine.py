@@ -101,10 +101,11 @@ class Engine:
 
     def __init__(self, ps: PhaseSpace, rc: float, rc_lj: Optional[float] = None,
                  periodic: Sequence[int] = (1, 1, 1), precision: str = "fp64", skin: float = 0.0,
-                 device: int = 0, capacity: int = 0, pair_scheme: str = "rows"):
+                 device: int = 0, capacity: int = 0, pair_scheme: str = "rows", arrays=None):
         """pair_scheme "rows": per-molecule candidate rows, each pair evaluated from both sides;
         "newton3": every pair evaluated once (Newton's third law, cluster pairs) where the system allows
-        it (one component of single-centre LJ molecules, mixed precision), rows elsewhere."""
+        it (one component of single-centre LJ molecules, mixed precision), rows elsewhere.  arrays: the
+        molecule arrays of ``abi.molecule_arrays(ps)`` to upload (e.g. page-locked copies), else made from ps."""
         self.L = load_library()
         self.ps = ps
         self.cfg = abi.make_config(ps.box, rc, rc if rc_lj is None else rc_lj, ps.eps_rf, periodic,
@@ -115,15 +116,15 @@ class Engine:
         self.tables = abi.ComponentTables(ps.components, ps.mixing)
         self._check(self.L.md_set_components(self.h, self.tables.array, self.tables.ncomp, self.tables.mixing),
                     "md_set_components")
-        self.upload(ps)
+        self.upload(ps, arrays)
 
     def _check(self, rc: int, what: str):
         if rc != abi.MD_OK:
             msg = self.L.md_last_error(self.h).decode() if self.h else ""
             raise EngineError(rc, f"{what}: {msg}")
 
-    def upload(self, ps: PhaseSpace):
-        ids, comp, r, v, q, Lm = abi.molecule_arrays(ps)
+    def upload(self, ps: PhaseSpace, arrays=None):
+        ids, comp, r, v, q, Lm = abi.molecule_arrays(ps) if arrays is None else arrays
         self.n = ps.n
         self._check(self.L.md_upload_molecules(self.h, ps.n, ids.ctypes.data, comp.ctypes.data, abi.dptr(r),
                                                abi.dptr(v), abi.dptr(q), abi.dptr(Lm)), "md_upload_molecules")
@@ -346,11 +347,14 @@ class Engine:
         self.write_phasespace_binary(name, time)
         return name
 
-    def molecules(self) -> dict:
+    def molecules(self, out: Optional[dict] = None) -> dict:
+        """All molecules in upload order; `out` (same keys, e.g. page-locked arrays from pinned.empty) receives
+        them instead of new arrays."""
         n = self.n
-        out = dict(ids=np.zeros(n, np.uint64), comp=np.zeros(n, np.int32), r=np.zeros((n, 3)), v=np.zeros((n, 3)),
-                   q=np.zeros((n, 4)), L=np.zeros((n, 3)), F=np.zeros((n, 3)), M=np.zeros((n, 3)),
-                   Vi=np.zeros((n, 3)))
+        if out is None:
+            out = dict(ids=np.zeros(n, np.uint64), comp=np.zeros(n, np.int32), r=np.zeros((n, 3)),
+                       v=np.zeros((n, 3)), q=np.zeros((n, 4)), L=np.zeros((n, 3)), F=np.zeros((n, 3)),
+                       M=np.zeros((n, 3)), Vi=np.zeros((n, 3)))
         self._check(self.L.md_download_molecules(self.h, n, *(out[k].ctypes.data for k in
                                                               ("ids", "comp", "r", "v", "q", "L", "F", "M", "Vi"))),
                     "md_download_molecules")
