@@ -149,6 +149,15 @@ const char* md_last_error(const md_ctx* ctx);
 /* mixing: ncomp*(ncomp-1)/2 rows of (xi, eta) for the pairs (i<j) in row order. */
 int md_set_components(md_ctx* ctx, const md_component* comps, int32_t ncomp, const double* mixing);
 
+/* Forces, torques and per-molecule virials (n x 3 each, in the order of the
+ * last upload; NULL leaves a quantity unchanged), for a caller that uploaded
+ * molecules between the force evaluation and the next pre-force half step --
+ * ls1's host molecules after a plugin edited them through the container's
+ * iterator -- since the pre-force half step kicks with the forces of the
+ * last evaluation (FullMolecule::upd_preF, FullMolecule.cpp:331-361) and an
+ * upload clears them. */
+int md_set_forces(md_ctx* ctx, int64_t n, const double* F, const double* M, const double* Vi);
+
 /* r, v, L: n x 3; q: n x 4 (w, x, y, z); comp: 0-based component index. */
 int md_upload_molecules(md_ctx* ctx, int64_t n, const uint64_t* id, const int32_t* comp,
                         const double* r, const double* v, const double* q, const double* L);

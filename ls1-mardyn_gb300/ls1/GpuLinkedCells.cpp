@@ -5,6 +5,10 @@
 
 #include <sstream>
 
+#if defined(_OPENMP)
+#include <omp.h>
+#endif
+
 #include "Domain.h"
 #include "Simulation.h"
 #include "ensemble/EnsembleBase.h"
@@ -127,7 +131,7 @@ void GpuLinkedCells::ensureDevice() {
 void GpuLinkedCells::upload() {
 	std::vector<uint64_t> id;
 	std::vector<int32_t> comp;
-	std::vector<double> r, v, q, L;
+	std::vector<double> r, v, q, L, F, M, Vi;
 	_ids.clear();
 	_slot.clear();
 	for (auto m = LinkedCells::iterator(ParticleIterator::ONLY_INNER_AND_BOUNDARY); m.isValid(); ++m) {
@@ -142,36 +146,98 @@ void GpuLinkedCells::upload() {
 		}
 		const Quaternion qq = m->q();
 		q.insert(q.end(), {qq.qw(), qq.qx(), qq.qy(), qq.qz()});
+		for (int d = 0; d < 3; ++d) {
+			F.push_back(m->F(d));
+			M.push_back(m->M(d));
+			Vi.push_back(m->Vi(d));
+		}
 	}
 	check(md_upload_molecules(_ctx, (int64_t)id.size(), id.data(), comp.data(), r.data(), v.data(), q.data(),
 							  L.data()),
 		  "md_upload_molecules");
+	// the next pre-force half step kicks with these (the upload clears the device's)
+	check(md_set_forces(_ctx, (int64_t)id.size(), F.data(), M.data(), Vi.data()), "md_set_forces");
 	_deviceStale = false;
 	_hostStale = false;
 }
 
-void GpuLinkedCells::syncToHost() {
-	if (!_ctx || !_hostStale) return;
+// The device state into host buffers (upload order).
+void GpuLinkedCells::downloadState() {
 	const size_t n = _ids.size();
-	std::vector<double> r(3 * n), v(3 * n), q(4 * n), L(3 * n), F(3 * n), M(3 * n), Vi(3 * n);
-	check(md_download_molecules(_ctx, (int64_t)n, nullptr, nullptr, r.data(), v.data(), q.data(), L.data(),
-								F.data(), M.data(), Vi.data()),
+	for (auto* b : {&_dr, &_dv, &_dL, &_dF, &_dM, &_dVi}) b->resize(3 * n);
+	_dq.resize(4 * n);
+	check(md_download_molecules(_ctx, (int64_t)n, nullptr, nullptr, _dr.data(), _dv.data(), _dq.data(), _dL.data(),
+								_dF.data(), _dM.data(), _dVi.data()),
 		  "md_download_molecules");
+}
+
+// The downloaded values into the mirror molecules the container's iterator
+// hands this thread (all of them outside a parallel region), copies of which
+// go to `out`.
+void GpuLinkedCells::applyDownload(std::vector<Molecule>& out) {
 	for (auto m = LinkedCells::iterator(ParticleIterator::ONLY_INNER_AND_BOUNDARY); m.isValid(); ++m) {
 		const size_t k = _slot.at(m->getID());
 		for (int d = 0; d < 3; ++d) {
-			m->setr(d, r[3 * k + d]);
-			m->setv(d, v[3 * k + d]);
-			m->setD(d, L[3 * k + d]);
+			m->setr(d, _dr[3 * k + d]);
+			m->setv(d, _dv[3 * k + d]);
+			m->setD(d, _dL[3 * k + d]);
 		}
-		m->setq(Quaternion(q[4 * k], q[4 * k + 1], q[4 * k + 2], q[4 * k + 3]));
-		m->setF(&F[3 * k]);
-		m->setM(&M[3 * k]);
-		m->setVi(&Vi[3 * k]);
+		m->setq(Quaternion(_dq[4 * k], _dq[4 * k + 1], _dq[4 * k + 2], _dq[4 * k + 3]));
+		m->setF(&_dF[3 * k]);
+		m->setM(&_dM[3 * k]);
+		m->setVi(&_dVi[3 * k]);
+		out.push_back(*m);
 	}
+}
+
+// Re-bin the mirror from scratch: since the last sync a molecule may have
+// crossed a periodic boundary on the device (its position wrapped to the far
+// side), which LinkedCells::update, built for moves of at most one cell, does
+// not handle; the halo cells stay empty until the host rebuilds them.
+void GpuLinkedCells::rebinMirror(std::vector<Molecule>& mols) {
+	LinkedCells::clear();
+	LinkedCells::addParticles(mols);
+	mols.clear();
 	_hostStale = false;
-	LinkedCells::update();  // positions moved: re-bin the mirror
-	_deviceStale = true;    // the caller may now edit molecules through the iterator
+	_deviceStale = true;  // the caller may now edit molecules through the iterator
+}
+
+void GpuLinkedCells::syncToHost() {
+	if (!_ctx || !_hostStale) return;
+	downloadState();
+	std::vector<Molecule> mols;
+	mols.reserve(_ids.size());
+	applyDownload(mols);
+	rebinMirror(mols);
+}
+
+// ls1 iterates the container inside OpenMP parallel regions, every thread of
+// the team asking for its own iterator, which covers that thread's share of
+// the cells (e.g. Leapfrog.cpp:84-125, Domain.cpp:457-480): the download is
+// done by one thread, every thread then updates its share of the mirror, and
+// one thread re-bins it; the barriers keep the team from iterating a mirror
+// that is not complete.
+void GpuLinkedCells::syncForIteration() {
+#if defined(_OPENMP)
+	if (omp_in_parallel()) {
+		bool need = false;
+		#pragma omp single copyprivate(need)
+		{
+			need = _ctx != nullptr && _hostStale;
+			if (need) downloadState();
+		}
+		if (!need) return;
+		std::vector<Molecule> mine;
+		applyDownload(mine);
+		#pragma omp critical(gpu_linked_cells_sync)
+		_pending.insert(_pending.end(), mine.begin(), mine.end());
+		#pragma omp barrier
+		#pragma omp single
+		rebinMirror(_pending);
+		return;
+	}
+#endif
+	syncToHost();
 }
 
 md_ctx* GpuLinkedCells::deviceContext() {
@@ -194,13 +260,13 @@ void GpuLinkedCells::traverseCells(CellProcessor& cellProcessor) {
 }
 
 ParticleIterator GpuLinkedCells::iterator(ParticleIterator::Type t) {
-	syncToHost();
+	syncForIteration();
 	return LinkedCells::iterator(t);
 }
 
 RegionParticleIterator GpuLinkedCells::regionIterator(const double startCorner[3], const double endCorner[3],
 													  ParticleIterator::Type t) {
-	syncToHost();
+	syncForIteration();
 	return LinkedCells::regionIterator(startCorner, endCorner, t);
 }
 

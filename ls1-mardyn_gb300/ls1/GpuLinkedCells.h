@@ -52,6 +52,10 @@ public:
 										  ParticleIterator::Type t) override;
 	unsigned long getNumberOfParticles(ParticleIterator::Type t = ParticleIterator::ALL_CELLS) override;
 	std::string getName() override { return "GpuLinkedCells"; }
+	/* Every pair's force reaches both molecules on the device (no force
+	 * exchange of halo copies, ParticleContainer.h:232); LinkedCells would ask
+	 * its traversal tuner, which never runs here. */
+	bool requiresForceExchange() const override { return false; }
 
 	/* Used by GpuLeapfrog: the device context (uploading the mirror first if
 	 * it was edited) and the notice that the device state moved on. */
@@ -65,6 +69,10 @@ private:
 	void ensureDevice();
 	void upload();
 	void syncToHost();
+	void syncForIteration();
+	void downloadState();
+	void applyDownload(std::vector<Molecule>& out);
+	void rebinMirror(std::vector<Molecule>& mols);
 	void check(int rc, const char* what) const;
 
 	md_ctx* _ctx = nullptr;
@@ -76,4 +84,6 @@ private:
 	bool _deviceStale = true;   // host mirror edited since the last upload
 	std::vector<unsigned long> _ids;                 // upload order
 	std::unordered_map<unsigned long, size_t> _slot; // id -> upload index
+	std::vector<double> _dr, _dv, _dq, _dL, _dF, _dM, _dVi;  // the last download (upload order)
+	std::vector<Molecule> _pending;                  // mirror molecules gathered by the team for the re-bin
 };

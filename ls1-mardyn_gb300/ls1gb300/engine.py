@@ -53,6 +53,7 @@ def load_library(path: str = LIB_PATH):
     L.md_set_components.argtypes = [vp, C.POINTER(abi.MdComponent), i32, dp]
     L.md_upload_molecules.argtypes = [vp, i64, vp, vp, dp, dp, dp, dp]
     L.md_download_molecules.argtypes = [vp, i64] + [vp] * 9
+    L.md_set_forces.argtypes = [vp, i64, vp, vp, vp]
     L.md_rebin_and_halo.argtypes = [vp, C.POINTER(abi.MdBinStats)]
     L.md_get_cell_assignment.argtypes = [vp, i64, vp]
     L.md_compute_forces.argtypes = [vp, C.POINTER(abi.MdForcesOut)]
@@ -128,6 +129,14 @@ class Engine:
         self.n = ps.n
         self._check(self.L.md_upload_molecules(self.h, ps.n, ids.ctypes.data, comp.ctypes.data, abi.dptr(r),
                                                abi.dptr(v), abi.dptr(q), abi.dptr(Lm)), "md_upload_molecules")
+
+    def set_forces(self, F: Optional[np.ndarray] = None, M: Optional[np.ndarray] = None,
+                   Vi: Optional[np.ndarray] = None):
+        """Forces, torques and per-molecule virials (n x 3, upload order) into the state, e.g. after a
+        re-upload of edited molecules, whose next pre-force half step kicks with them."""
+        arrs = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (F, M, Vi)]
+        self._check(self.L.md_set_forces(self.h, self.n, *(None if a is None else a.ctypes.data for a in arrs)),
+                    "md_set_forces")
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:

@@ -267,6 +267,14 @@ int orc_set_molecules(orc_sys* s, int64_t n, const uint64_t* id, const int32_t* 
 
 int64_t orc_num_molecules(const orc_sys* s) { return s->n; }
 
+int orc_set_forces(orc_sys* s, int64_t n, const double* F, const double* M, const double* Vi) {
+    if (n != s->n) return MD_ERR_ARG;
+    if (F) memcpy(s->F, F, sizeof(double) * 3 * n);
+    if (M) memcpy(s->M, M, sizeof(double) * 3 * n);
+    if (Vi) memcpy(s->Vi, Vi, sizeof(double) * 3 * n);
+    return MD_OK;
+}
+
 int orc_get_molecules(const orc_sys* s, int64_t n, uint64_t* id, int32_t* comp, double* r, double* v, double* q,
                       double* L, double* F, double* M, double* Vi) {
     if (n != s->n) return MD_ERR_ARG;

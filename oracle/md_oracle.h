@@ -29,6 +29,8 @@ int orc_set_threads(int32_t n);
 int orc_set_molecules(orc_sys* s, int64_t n, const uint64_t* id, const int32_t* comp, const double* r,
                       const double* v, const double* q, const double* L);
 int64_t orc_num_molecules(const orc_sys* s);
+/* F, M, Vi (n x 3, molecule order; NULL: unchanged) */
+int orc_set_forces(orc_sys* s, int64_t n, const double* F, const double* M, const double* Vi);
 int orc_get_molecules(const orc_sys* s, int64_t n, uint64_t* id, int32_t* comp, double* r, double* v,
                       double* q, double* L, double* F, double* M, double* Vi);
 /* wrap leavers (periodic dims), bin, build halo copies, build site caches */

@@ -255,6 +255,43 @@ def psm_small():
     return psm.lj_fcc(4, 0.8, 1.0, seed=3)   # L = 6.84: two list cells of edge >= 2.75 per axis
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_reupload_with_set_forces_continues_the_run(engine_mod, precision):
+    """A caller that downloads, edits nothing and re-uploads the molecules
+    between the force evaluation and the next pre-force half step (ls1's
+    host mirror after a plugin iterated it) hands the forces back with
+    md_set_forces; the step that follows equals the one without the round
+    trip (FP64: bit for bit)."""
+    ps, g = golden_io.load("per_mix500")
+    a = engine_mod.Engine(ps, g["rc"], g["rc_lj"], precision=precision)
+    b = engine_mod.Engine(ps, g["rc"], g["rc_lj"], precision=precision)
+    dt = 5e-5
+    for e in (a, b):
+        e.forces()
+        e.pre(dt)
+        e.forces()
+        e.post(dt)
+    m = b.molecules()
+    q = ps.copy()
+    o = _by_id(m["ids"])
+    q.r, q.v, q.q, q.L, q.ids, q.comp = m["r"][o], m["v"][o], m["q"][o], m["L"][o], m["ids"][o], m["comp"][o]
+    b.upload(q)
+    b.set_forces(m["F"][o], m["M"][o], m["Vi"][o])
+    for e in (a, b):
+        e.pre(dt)
+        e.forces()
+        e.post(dt)
+    ma, mb = a.molecules(), b.molecules()
+    a.close()
+    b.close()
+    ia, ib = _by_id(ma["ids"]), _by_id(mb["ids"])
+    for k in ("r", "v", "q", "L", "F"):
+        if precision == "fp64":
+            np.testing.assert_array_equal(ma[k][ia], mb[k][ib], k)
+        else:
+            assert np.abs(ma[k][ia] - mb[k][ib]).max() <= 1e-6 * max(np.abs(ma[k]).max(), 1e-300), k
+
+
 def test_mixed_matches_fp64_at_scale(engine_mod):
     """1CLJ N=32000 (the reference's small benchmark case): mixed-precision
     forces within 1e-5 relative rms of the FP64 kernel, Upot within 1e-6."""
