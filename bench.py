@@ -432,8 +432,9 @@ def _perturbed(ps, f: float):
 
 def run_adjoint(a, rank, world, local, pg):
     """Forward and adjoint cost on the differentiation workload: 64 snapshots
-    each of 1CLJ (fcc 29^3 x 4 = 97,556 molecules, rho*=0.7, T*=1.1, rc=2.5) and
-    of the 2CLJQ/1CLJD mixture (97,556 molecules on the same lattice, rc=1 nm).  Per snapshot the loss is
+    each of 1CLJ (100,000 molecules: fcc 30^3 x 4 with 8,000 seeded vacancies,
+    rho*=0.7, T*=1.1, rc=2.5) and of the 2CLJQ/1CLJD mixture (100,000 molecules
+    the same way, 18 nm^-3, rc=1 nm).  Per snapshot the loss is
     L = (U - U*)^2 + w (P - P*)^2 with targets from the FP64 forward at +2 %
     parameters; the forward is md_compute_forces (list build + pair kernel +
     sums), the adjoint md_adjoint (pairs recomputed from the list; gradients
@@ -441,11 +442,11 @@ def run_adjoint(a, rank, world, local, pg):
     FP64 accumulation."""
     from ls1gb300 import engine as E
     cu = Cudart()
-    mix = psm.mixture(100_000, 18.0, 300.0, seed=4)
-    systems = [("1CLJ fcc 29^3x4 = 97,556, rho*=0.7, T*=1.1, rc=2.5",
-                psm.lj_fcc(29, 0.7, 1.1, seed=4), 2.5, 0.002, 0.3),
-               (f"2CLJQ/1CLJD mixture on fcc 29^3x4 = {mix.n:,} sites (n=18 nm^-3, T=300 K, rc=1 nm)",
-                mix, 1.0, 9.118e-5, 0.1)]
+    systems = [("1CLJ N=100,000 (fcc 30^3x4 with 8,000 vacancies), rho*=0.7, T*=1.1, rc=2.5",
+                psm.with_vacancies(psm.lj_fcc(30, 0.7, 1.1, seed=4), 100_000, 0.7, 4), 2.5, 0.002, 0.3),
+               ("2CLJQ/1CLJD mixture N=100,000 (fcc 30^3x4 with 8,000 vacancies), n=18 nm^-3, T=300 K, rc=1 nm",
+                psm.with_vacancies(psm.mixture(108_000, 18.0, 300.0, seed=4), 100_000, 18.0, 4), 1.0, 9.118e-5,
+                0.1)]
     out = []
     for desc, ps, rc, dt, skin in systems:
         n = ps.n
@@ -495,8 +496,8 @@ def run_adjoint(a, rank, world, local, pg):
         print(json.dumps({"metric": "adjoint/forward cost", "value": max(o["adjoint_over_forward"] for o in out),
                           "unit": "ratio", "higher_is_better": False, "n_gpus": world,
                           "dtype": "f32-pairs/f64-accumulation", "data": "synthetic (seeded snapshots of NVE runs)",
-                          "config": {"workload": "64 snapshots each of 1CLJ N=97,556 and the 2CLJQ/1CLJD mixture "
-                                                 "N=97,556; loss (U-U*)^2 + w (P-P*)^2, targets from FP64 at +2 % "
+                          "config": {"workload": "64 snapshots each of 1CLJ N=100,000 and the 2CLJQ/1CLJD mixture "
+                                                 "N=100,000; loss (U-U*)^2 + w (P-P*)^2, targets from FP64 at +2 % "
                                                  "parameters; CUDA events on the engine stream",
                                      "value": "max over the two systems of adjoint pair-kernel time / forward "
                                               "pair-kernel time on the same list; call_* are the whole ABI calls "
@@ -667,10 +668,10 @@ def main():
                    "pair_kernel_ms": kt3.force_ms, "half_steps_ms": kt3.lf_ms, "rebuild_ms": kt3.rebuild_ms,
                    "rebuilds_timed": int(rb3), "list_entries_per_molecule": kt3.mean_candidates,
                    "pair_kernel_tflops": a3, "pair_kernel_frac_fp32": a3 / fp32_peak}
-    # the adjoint on the differentiation workload's mixture (2CLJQ/1CLJD, ~100,000 molecules)
+    # the adjoint on the differentiation workload's mixture (2CLJQ/1CLJD, 100,000 molecules)
     adj_mix = None
     if a.workload == "lj4m" and a.precision == "mixed" and not rmm:
-        mps = psm.mixture(100_000, 18.0, 300.0, seed=4)
+        mps = psm.with_vacancies(psm.mixture(108_000, 18.0, 300.0, seed=4), 100_000, 18.0, 4)
         em = E.Engine(mps, 1.0, precision="mixed", skin=0.1, device=local)
         em.forces()
         ktm = em.time_kernels(5)

@@ -300,6 +300,27 @@ def lj_fcc(cells: int, rho: float, T: float, seed: int, shifted: bool = False, r
                       np.zeros((n, 3)), T)
 
 
+def with_vacancies(ps: PhaseSpace, n: int, density: float, seed: int) -> PhaseSpace:
+    """Exactly ``n`` molecules of a lattice state at number density
+    ``density``: a seeded random choice of n of its molecules (order kept,
+    ids renumbered 1..n), box and positions scaled so that n / V = density,
+    and the net momentum of the kept molecules removed again."""
+    if not 0 < n <= ps.n:
+        raise ValueError("n must lie in (0, ps.n]")
+    keep = np.sort(np.random.default_rng(seed).choice(ps.n, n, replace=False))
+    q = ps.copy()
+    s = (n / density / float(np.prod(ps.box))) ** (1.0 / 3.0)
+    q.box = np.asarray(ps.box, np.float64) * s
+    q.r = ps.r[keep] * s
+    q.comp = ps.comp[keep].copy()
+    masses = np.array([c.mass_inertia()[0] for c in ps.components])[q.comp]
+    v = ps.v[keep]
+    q.v = v - ((v * masses[:, None]).sum(axis=0) / masses.sum())[None, :]
+    q.q, q.L = ps.q[keep].copy(), ps.L[keep].copy()
+    q.ids = np.arange(1, n + 1, dtype=np.uint64)
+    return q
+
+
 def lj_slab(cells_xy: int, rho_liq: float, rho_vap: float, T: float, seed: int,
             elongation: float = 3.0) -> PhaseSpace:
     """Vapour-liquid slab: an fcc liquid at rho_liq filling the middle third of

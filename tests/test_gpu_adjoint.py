@@ -1,9 +1,13 @@
 """Adjoint of the force field (md_adjoint) against FP64 central finite
-differences of the engine's own FP64 forward, against an FP64 all-pairs torch
-reference, and through a torch.autograd.Function used only here (validation
-harness).  Tolerances: parameter and position gradients 1e-6 relative to the
-largest component (FP64 adjoint), 2e-4 (FP32 pair arithmetic, FP64 sums)."""
+differences of the C oracle's forward (the restatement pinned against the
+reference) and of the engine's own FP64 forward, against FP64 all-pairs torch
+references (1CLJ here; the 2CLJQ + 1CLJD mixture through oracle/allpairs.py,
+written from the textbook multipole energies), and through a
+torch.autograd.Function used only here (validation harness).  Tolerances:
+parameter and position gradients 1e-6 relative to the largest component
+(FP64 adjoint) unless stated, 2e-4 (FP32 pair arithmetic, FP64 sums)."""
 import copy
+import os
 
 import numpy as np
 import pytest
@@ -133,6 +137,66 @@ def test_mixed_precision_adjoint_close_to_fp64(E):
     gr32, gp32 = out["mixed"]
     assert np.abs(gp32 - gp64).max() <= 2e-4 * np.abs(gp64).max()
     assert np.sqrt(((gr32 - gr64) ** 2).mean()) <= 2e-4 * np.sqrt((gr64 ** 2).mean())
+
+
+def _oracle_uw(ps, rc):
+    from oracle.oracle import Oracle
+    o = Oracle(ps, rc, threads=min(os.cpu_count() or 1, 16))
+    o.rebin()
+    fo, _ = o.forces()
+    return fo.upot, fo.virial
+
+
+def _system(name):
+    if name == "lj":
+        return lj_box(), 2.5
+    return psm.mixture(2000, 14.0, 300.0, seed=4), 1.0
+
+
+@pytest.mark.parametrize("name", ["lj", "mixture"])
+def test_parameter_gradients_vs_oracle_finite_differences(E, name):
+    """dUpot/dp and dvirial/dp for every site parameter (eps and sigma of each
+    LJ centre, |Q| of the quadrupole, |mu| of the dipole) against central
+    differences of the oracle's FP64 forward with the parameter perturbed by
+    h = 1e-5 |p| (the differences agree with the all-pairs reference to about
+    1e-9 at this step)."""
+    ps, rc = _system(name)
+    e, U, W = forward(E, ps, rc)
+    _, gpU = e.adjoint(1.0, 0.0)
+    _, gpW = e.adjoint(0.0, 1.0)
+    U0, W0 = _oracle_uw(ps, rc)
+    assert abs(U - U0) <= 1e-10 * abs(U0) and abs(W - W0) <= 1e-10 * abs(W0)
+    for k in range(e.param_count()):
+        p0 = get_param(ps, k)
+        h = 1e-5 * abs(p0)
+        Up, Wp = _oracle_uw(set_param(ps, k, p0 + h), rc)
+        Um, Wm = _oracle_uw(set_param(ps, k, p0 - h), rc)
+        fu, fw = (Up - Um) / (2 * h), (Wp - Wm) / (2 * h)
+        assert abs(gpU[k] - fu) <= 5e-8 * abs(fu), (k, gpU[k], fu)
+        assert abs(gpW[k] - fw) <= 5e-8 * abs(fw), (k, gpW[k], fw)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 2e-4)])
+def test_mixture_against_fp64_all_pairs_torch_reference(E, precision, tol):
+    """2,048-molecule 2CLJQ + 1CLJD mixture: position gradients (with a force
+    cotangent gF, i.e. the pair Hessian-vector products of the LJ, dipole and
+    quadrupole bodies) and parameter gradients of the adjoint against the FP64
+    all-pairs torch reference, for three (gU, gW, gF) combinations.  FP64:
+    per parameter 1e-9 relative; mixed: 2e-4 of the largest."""
+    pytest.importorskip("torch")
+    from oracle.allpairs import AllPairs
+    ps, rc = _system("mixture")
+    ap = AllPairs(ps, rc)
+    gF = np.random.default_rng(17).normal(size=(ps.n, 3))
+    e, U, W = forward(E, ps, rc, precision)
+    for gU, gW, g in ((1.0, 0.0, None), (0.0, 1.0, None), (0.3, -0.2, gF)):
+        gr, gp = e.adjoint(gU, gW, g)
+        gr_t, gp_t, Ut, Wt = ap.gradients(gU, gW, g)
+        if precision == "fp64":
+            assert abs(U - Ut) <= 1e-10 * abs(Ut) and abs(W - Wt) <= 1e-10 * abs(Wt)
+        assert np.abs(gr - gr_t).max() <= tol * np.abs(gr_t).max(), (gU, gW, np.abs(gr - gr_t).max())
+        scale = np.abs(gp_t) if precision == "fp64" else np.abs(gp_t).max()
+        assert np.all(np.abs(gp - gp_t) <= tol * scale), (gU, gW, gp, gp_t)
 
 
 @pytest.mark.parametrize("shifted", [False, True])
