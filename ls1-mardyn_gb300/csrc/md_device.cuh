@@ -19,6 +19,7 @@
 
 #define MD_MAXC 8          // components
 #define MD_MAXS 8          // sites per component
+#define MD_SITE_VEC 4      // elements per site record of the site caches: x, y, z and one pad (16-byte float records)
 #define MD_MAXLJ 32        // LJ centres over all components
 #define MD_CODE_SHIFT 27
 #define MD_INDEX_MASK ((1u << MD_CODE_SHIFT) - 1u)

@@ -817,10 +817,10 @@ __global__ void k_sites(State S, Real* sd, Real* se, int stride) {
     for (int k = 0; k < C.ns; ++k) {
         double o[3];
         qrot(w, x, y, z, C.d[k], o);
-        for (int e = 0; e < 3; ++e) sd[((int64_t)i * stride + k) * 3 + e] = (Real)o[e];
+        for (int e = 0; e < 3; ++e) sd[((int64_t)i * stride + k) * MD_SITE_VEC + e] = (Real)o[e];
         if (C.kind[k] >= SK_DIPOLE) {
             qrot(w, x, y, z, C.e[k], o);
-            for (int e = 0; e < 3; ++e) se[((int64_t)i * stride + k) * 3 + e] = (Real)o[e];
+            for (int e = 0; e < 3; ++e) se[((int64_t)i * stride + k) * MD_SITE_VEC + e] = (Real)o[e];
         }
     }
 }
@@ -1394,6 +1394,18 @@ __global__ void k_row_partition(int64_t n, const float4* __restrict__ xl, uint32
     }
 }
 
+// x, y, z of one site record of the site caches (one 16-byte load in FP32,
+// a 16-byte and an 8-byte load in FP64; records are MD_SITE_VEC-aligned).
+template <typename Real> __device__ __forceinline__ void site_rec(const Real* p, Real* o);
+template <> __device__ __forceinline__ void site_rec<float>(const float* p, float* o) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    o[0] = v.x; o[1] = v.y; o[2] = v.z;
+}
+template <> __device__ __forceinline__ void site_rec<double>(const double* p, double* o) {
+    const double2 v = __ldg(reinterpret_cast<const double2*>(p));
+    o[0] = v.x; o[1] = v.y; o[2] = __ldg(p + 2);
+}
+
 // Centre distance m_d = r_i - (r_j + image) of candidate e: FP32 local
 // coordinates with the cell offset (mixed precision) or FP64 positions with
 // the reference's halo shift.
@@ -1515,6 +1527,7 @@ __device__ __forceinline__ void warp_partial_acc(double* partials, int pstride, 
 }
 
 #define MS_WARPS 4     // warps per block of the multi-site kernels
+static_assert(MD_SITE_VEC * MD_MAXS <= 32, "one lane per element loads the warp molecule's site records");
 #define MS_MOLS 32     // molecules per warp, one after another
 #ifndef MS_MIN_BLOCKS
 #define MS_MIN_BLOCKS 5  // FP32 variants: blocks per SM the register budget is sized for (96 registers, no spills)
@@ -1543,9 +1556,10 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
     const int64_t w = (int64_t)blockIdx.x * MS_WARPS + wl;
     typename Acc<Real>::type u6, ux, vir, rf;
     u6.init(); ux.init(); vir.init(); rf.init();
-    int cnt_pairs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // pair counts by kind (molecule pairs, LJ, C-C, C-D, D-D, C-Q, D-Q, Q-Q), in registers
+    int n_mol = 0, n_lj = 0, n_cc = 0, n_cd = 0, n_dd = 0, n_cq = 0, n_dq = 0, n_qq = 0;
     const Real epsRF = (Real)cP.epsRFInvrc3;
-    const uint32_t sstride = 3u * (uint32_t)stride;  // site arrays are [slot][site][3]; the host keeps cap * stride * 3 < 2^32
+    const uint32_t sstride = MD_SITE_VEC * (uint32_t)stride;  // site records [slot][site][MD_SITE_VEC]; the host keeps cap * stride * MD_SITE_VEC < 2^32
     for (int t = 0; t < MS_MOLS; ++t) {
         const int64_t i = w * MS_MOLS + t;
         if (i >= S.n) break;  // warp-uniform
@@ -1559,66 +1573,143 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
             pi[0] = S.rx[i]; pi[1] = S.ry[i]; pi[2] = S.rz[i];
         }
         __syncwarp();
-        if (lane < 3 * A.ns) {
-            site_i[wl][0][lane / 3][lane % 3] = sd[(uint32_t)i * sstride + lane];
-            site_i[wl][1][lane / 3][lane % 3] = se[(uint32_t)i * sstride + lane];
+        if (lane < MD_SITE_VEC * A.ns && lane % MD_SITE_VEC < 3) {  // MD_SITE_VEC * MD_MAXS = 32 lanes
+            site_i[wl][0][lane / MD_SITE_VEC][lane % MD_SITE_VEC] = sd[(uint32_t)i * sstride + lane];
+            site_i[wl][1][lane / MD_SITE_VEC][lane % MD_SITE_VEC] = se[(uint32_t)i * sstride + lane];
         }
         __syncwarp();
         typename Acc<Real>::type F[3], M[3], V[3];
         for (int c = 0; c < 3; ++c) { F[c].init(); M[c].init(); V[c].init(); }
+        // One molecule pair: the site pairs in blocks by kind (LJ x LJ, then each
+        // electrostatic site of i against the charges, dipoles and quadrupoles
+        // of j), so that every block has one body and warp-uniform trip counts
+        // where the neighbours share a component.  The i-site forces are summed
+        // per site before its lever-arm torque; the virial of the molecule
+        // pair is m_d o (sum of its site forces).
         auto body = [&](uint32_t e, int fl, const Real* md) {
             const uint32_t j = e & MD_INDEX_MASK;
-            const bool lj_on = fl & 1, el_on = (fl & 2) != 0;
             const int cj = S.comp[j];
             const CompDev& B = cP.comp[cj];
             const bool macro = (int64_t)j > i;
-            // this molecule pair's contributions, added to the compensated sums once
-            Real fp[3] = {0, 0, 0}, mp[3] = {0, 0, 0}, vp[3] = {0, 0, 0};
+            const uint32_t jb = j * sstride;
+            Real fp[3] = {0, 0, 0}, mp[3] = {0, 0, 0};
             Real u6p = 0, uxp = 0, rfp = 0;
-            for (int a = 0; a < A.ns; ++a) {
-                const int ka = A.kind[a];
-                if (ka == SK_LJ && !lj_on) continue;
-                if (ka != SK_LJ && !el_on) continue;
-                const Real* da = site_i[wl][0][a];
-                const Real* ea = site_i[wl][1][a];
-                Real fa[3] = {0, 0, 0}, ta[3] = {0, 0, 0};
-                for (int b = 0; b < B.ns; ++b) {
-                    const int kb = B.kind[b];
-                    if ((ka == SK_LJ) != (kb == SK_LJ)) continue;
-                    const uint32_t ob = j * sstride + 3u * (uint32_t)b;
-                    Real db[3], eb[3] = {0, 0, 0};
-                    for (int c = 0; c < 3; ++c) db[c] = sd[ob + c];
-                    if (kb >= SK_DIPOLE)
-                        for (int c = 0; c < 3; ++c) eb[c] = se[ob + c];
-                    Real dsite[3] = {md[0] + (da[0] - db[0]), md[1] + (da[1] - db[1]), md[2] + (da[2] - db[2])};
-                    Real f[3], Vp[3], T[3] = {0, 0, 0}, u = 0, urf = 0;
-                    int kind;
-                    if (ka == SK_LJ) {
-                        const int ga = A.ljoff + a, gb = B.ljoff + b;
-                        const Real s2r = dsite[0] * dsite[0] + (dsite[1] * dsite[1] + dsite[2] * dsite[2]);
-                        lj_pair<Real>(dsite, md, s2r, PTab<Real>::eps24(cP, ga * cP.nlj + gb),
-                                      PTab<Real>::sig2(cP, ga * cP.nlj + gb), PTab<Real>::shift6(cP, ga * cP.nlj + gb), f,
-                                      Vp, u);
+            if (fl & 1) {
+                const int nlb = B.nlj;
+                for (int a = 0; a < A.nlj; ++a) {
+                    const Real* da = site_i[wl][0][a];
+                    const int row = (A.ljoff + a) * cP.nlj + B.ljoff;
+                    Real fa[3] = {0, 0, 0};
+                    for (int b = 0; b < nlb; ++b) {
+                        Real db[3];
+                        site_rec<Real>(sd + jb + MD_SITE_VEC * (uint32_t)b, db);
+                        const Real ds[3] = {md[0] + (da[0] - db[0]), md[1] + (da[1] - db[1]), md[2] + (da[2] - db[2])};
+                        const Real s2r = ds[0] * ds[0] + (ds[1] * ds[1] + ds[2] * ds[2]);
+                        Real f[3], Vd[3], u;
+                        lj_pair<Real>(ds, md, s2r, PTab<Real>::eps24(cP, row + b), PTab<Real>::sig2(cP, row + b),
+                                      PTab<Real>::shift6(cP, row + b), f, Vd, u);
+                        fa[0] += f[0]; fa[1] += f[1]; fa[2] += f[2];
                         u6p += u;
-                        kind = 0;
-                    } else {
-                        kind = multipole_pair<Real>(ka, kb, dsite, md, PTab<Real>::p(cP, ci, a), ea,
-                                                    PTab<Real>::p(cP, cj, b), eb, epsRF, f, Vp, T, u, urf);
-                        uxp += u;
-                        rfp += urf;
                     }
-                    for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; vp[c] += Vp[c]; }
-                    if (macro) cnt_pairs[1 + kind] += 1;
+                    mp[0] += da[1] * fa[2] - da[2] * fa[1];
+                    mp[1] += da[2] * fa[0] - da[0] * fa[2];
+                    mp[2] += da[0] * fa[1] - da[1] * fa[0];
+                    fp[0] += fa[0]; fp[1] += fa[1]; fp[2] += fa[2];
                 }
-                // torque of the site forces about the centre plus the multipole torque
-                mp[0] += (da[1] * fa[2] - da[2] * fa[1]) + ta[0];
-                mp[1] += (da[2] * fa[0] - da[0] * fa[2]) + ta[1];
-                mp[2] += (da[0] * fa[1] - da[1] * fa[0]) + ta[2];
-                for (int c = 0; c < 3; ++c) fp[c] += fa[c];
+                if (macro) n_lj += A.nlj * nlb;
             }
+            if (fl & 2) {
+                const int b0 = B.nlj, b1 = b0 + B.nch, b2 = b1 + B.ndi, b3 = B.ns;
+                for (int a = A.nlj; a < A.ns; ++a) {
+                    const int ka = A.kind[a];  // warp-uniform: i is the warp's molecule
+                    const Real* da = site_i[wl][0][a];
+                    const Real* ea = site_i[wl][1][a];
+                    const Real pa = PTab<Real>::p(cP, ci, a);
+                    Real fa[3] = {0, 0, 0}, ta[3] = {0, 0, 0};
+                    auto site_j = [&](int b, Real* ds, Real* eb) {
+                        const uint32_t ob = jb + MD_SITE_VEC * (uint32_t)b;
+                        Real db[3];
+                        site_rec<Real>(sd + ob, db);
+                        site_rec<Real>(se + ob, eb);
+                        for (int c = 0; c < 3; ++c) ds[c] = md[c] + (da[c] - db[c]);
+                    };
+                    Real ds[3], eb[3], f[3], T[3], Tj[3], u, urf;
+                    if (ka == SK_CHARGE) {
+                        for (int b = b0; b < b1; ++b) {
+                            site_j(b, ds, eb);
+                            cc_body<Real>(ds, pa, PTab<Real>::p(cP, cj, b), f, u);
+                            for (int c = 0; c < 3; ++c) fa[c] += f[c];
+                            uxp += u;
+                        }
+                        for (int b = b1; b < b2; ++b) {
+                            site_j(b, ds, eb);
+                            cd_body<Real>(ds, pa, eb, PTab<Real>::p(cP, cj, b), f, Tj, u);
+                            for (int c = 0; c < 3; ++c) fa[c] += f[c];
+                            uxp += u;
+                        }
+                        for (int b = b2; b < b3; ++b) {
+                            site_j(b, ds, eb);
+                            cq_body<Real>(ds, pa, eb, PTab<Real>::p(cP, cj, b), f, Tj, u);
+                            for (int c = 0; c < 3; ++c) fa[c] += f[c];
+                            uxp += u;
+                        }
+                        if (macro) { n_cc += B.nch; n_cd += B.ndi; n_cq += B.nqu; }
+                    } else if (ka == SK_DIPOLE) {
+                        for (int b = b0; b < b1; ++b) {
+                            site_j(b, ds, eb);
+                            const Real nd[3] = {-ds[0], -ds[1], -ds[2]};
+                            cd_body<Real>(nd, PTab<Real>::p(cP, cj, b), ea, pa, f, T, u);
+                            for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
+                            uxp += u;
+                        }
+                        for (int b = b1; b < b2; ++b) {
+                            site_j(b, ds, eb);
+                            dd_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, cj, b), epsRF, f, T, u, urf);
+                            for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
+                            uxp += u;
+                            rfp += urf;
+                        }
+                        for (int b = b2; b < b3; ++b) {
+                            site_j(b, ds, eb);
+                            dq_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, cj, b), f, T, Tj, u);
+                            for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
+                            uxp += u;
+                        }
+                        if (macro) { n_cd += B.nch; n_dd += B.ndi; n_dq += B.nqu; }
+                    } else {
+                        for (int b = b0; b < b1; ++b) {
+                            site_j(b, ds, eb);
+                            const Real nd[3] = {-ds[0], -ds[1], -ds[2]};
+                            cq_body<Real>(nd, PTab<Real>::p(cP, cj, b), ea, pa, f, T, u);
+                            for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
+                            uxp += u;
+                        }
+                        for (int b = b1; b < b2; ++b) {
+                            site_j(b, ds, eb);
+                            const Real nd[3] = {-ds[0], -ds[1], -ds[2]};
+                            dq_body<Real>(nd, eb, PTab<Real>::p(cP, cj, b), ea, pa, f, Tj, T, u);
+                            for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
+                            uxp += u;
+                        }
+                        for (int b = b2; b < b3; ++b) {
+                            site_j(b, ds, eb);
+                            qq_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, cj, b), f, T, Tj, u);
+                            for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
+                            uxp += u;
+                        }
+                        if (macro) { n_cq += B.nch; n_dq += B.ndi; n_qq += B.nqu; }
+                    }
+                    // torque of the site force about the centre plus the multipole torque
+                    mp[0] += (da[1] * fa[2] - da[2] * fa[1]) + ta[0];
+                    mp[1] += (da[2] * fa[0] - da[0] * fa[2]) + ta[1];
+                    mp[2] += (da[0] * fa[1] - da[1] * fa[0]) + ta[2];
+                    fp[0] += fa[0]; fp[1] += fa[1]; fp[2] += fa[2];
+                }
+            }
+            const Real vp[3] = {md[0] * fp[0], md[1] * fp[1], md[2] * fp[2]};
             for (int c = 0; c < 3; ++c) { F[c].add(fp[c]); M[c].add(mp[c]); V[c].add(vp[c]); }
             if (macro) {
-                if (el_on) cnt_pairs[0] += 1;
+                if (fl & 2) n_mol += 1;
                 u6.add(u6p);
                 ux.add(uxp);
                 rf.add(rfp);
@@ -1639,7 +1730,9 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
     warp_partial_acc(partials, pstride, 1, ux, 1.f);
     warp_partial_acc(partials, pstride, 2, vir, 1.f);
     warp_partial_acc(partials, pstride, 3, rf, -1.f);
-    for (int sl = 0; sl < 8; ++sl) warp_partial_count(partials, pstride, 4 + sl, (float)cnt_pairs[sl]);
+    const int cnts[8] = {n_mol, n_lj, n_cc, n_cd, n_dd, n_cq, n_dq, n_qq};
+#pragma unroll
+    for (int sl = 0; sl < 8; ++sl) warp_partial_count(partials, pstride, 4 + sl, (float)cnts[sl]);
 }
 
 // ------------------------------------------------------------------ integration
