@@ -1513,6 +1513,13 @@ __device__ __forceinline__ double warp_total(const KSum& k, float scale = 1.f) {
     return f2d_exact(__fadd_rn(hi, lo));
 }
 __device__ __forceinline__ double warp_total(const DSum& k, float scale = 1.f) { return (double)scale * warp_sum(k.s); }
+// The same for a plain per-lane value.
+__device__ __forceinline__ double warp_total_plain(float x, float scale = 1.f) {
+    float hi = scale * x, lo = 0.f;
+    warp_twosum(hi, lo);
+    return f2d_exact(__fadd_rn(hi, lo));
+}
+__device__ __forceinline__ double warp_total_plain(double x, float scale = 1.f) { return (double)scale * warp_sum(x); }
 
 // Per-warp partial of a per-lane accumulator, times sign (+-1).
 __device__ __forceinline__ void warp_partial_acc(double* partials, int pstride, int slot, const KSum& k, float sign) {
@@ -1530,7 +1537,10 @@ __device__ __forceinline__ void warp_partial_acc(double* partials, int pstride, 
 static_assert(MD_SITE_VEC * MD_MAXS <= 32, "one lane per element loads the warp molecule's site records");
 #define MS_MOLS 32     // molecules per warp, one after another
 #ifndef MS_MIN_BLOCKS
-#define MS_MIN_BLOCKS 5  // FP32 variants: blocks per SM the register budget is sized for (96 registers, no spills)
+#define MS_MIN_BLOCKS 6  // FP32 force kernel: blocks per SM the register budget is sized for (80 registers, no spills)
+#endif
+#ifndef MS_ADJ_MIN_BLOCKS
+#define MS_ADJ_MIN_BLOCKS 5  // FP32 adjoint kernel: the same (96 registers, no spills)
 #endif
 
 // General multi-site molecules: all site pairs of every molecule pair inside
@@ -1578,8 +1588,9 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
             site_i[wl][1][lane / MD_SITE_VEC][lane % MD_SITE_VEC] = se[(uint32_t)i * sstride + lane];
         }
         __syncwarp();
-        typename Acc<Real>::type F[3], M[3], V[3];
-        for (int c = 0; c < 3; ++c) { F[c].init(); M[c].init(); V[c].init(); }
+        // per-lane sums of this molecule's force, torque and virial: a lane adds two or three molecule pairs,
+        // so plain sums; the lanes are combined by a compensated warp sum
+        Real F[3] = {0, 0, 0}, M[3] = {0, 0, 0}, V[3] = {0, 0, 0};
         // One molecule pair: the site pairs in blocks by kind (LJ x LJ, then each
         // electrostatic site of i against the charges, dipoles and quadrupoles
         // of j), so that every block has one body and warp-uniform trip counts
@@ -1707,7 +1718,7 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
                 }
             }
             const Real vp[3] = {md[0] * fp[0], md[1] * fp[1], md[2] * fp[2]};
-            for (int c = 0; c < 3; ++c) { F[c].add(fp[c]); M[c].add(mp[c]); V[c].add(vp[c]); }
+            for (int c = 0; c < 3; ++c) { F[c] += fp[c]; M[c] += mp[c]; V[c] += vp[c]; }
             if (macro) {
                 if (fl & 2) n_mol += 1;
                 u6.add(u6p);
@@ -1717,9 +1728,10 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
             }
         };
         ms_walk_row<Real>(S, xlf, soff, pi, i, nbr + (size_t)i * maxnb, nnb[i], ring[wl], lane, body);
-        const double fx = warp_total(F[0]), fy = warp_total(F[1]), fz = warp_total(F[2]);
-        const double mx = warp_total(M[0]), my = warp_total(M[1]), mz = warp_total(M[2]);
-        const double vx = warp_total(V[0], 0.5f), vy = warp_total(V[1], 0.5f), vz = warp_total(V[2], 0.5f);
+        const double fx = warp_total_plain(F[0]), fy = warp_total_plain(F[1]), fz = warp_total_plain(F[2]);
+        const double mx = warp_total_plain(M[0]), my = warp_total_plain(M[1]), mz = warp_total_plain(M[2]);
+        const double vx = warp_total_plain(V[0], 0.5f), vy = warp_total_plain(V[1], 0.5f),
+                     vz = warp_total_plain(V[2], 0.5f);
         if (lane == 0) {
             S.Fx[i] = fx; S.Fy[i] = fy; S.Fz[i] = fz;
             S.Mx[i] = mx; S.My[i] = my; S.Mz[i] = mz;
