@@ -386,6 +386,15 @@ def run_batch(a, rank, world, local, pg):
         upd += boxes[k].n * 100
         eng.close()
     seq = upd / (tot_ms * 1e-3)
+    # what one persistent launch per chunk could save: the graph's per-node launch cost (4 nodes per step: the
+    # rebuild test, the conditional rebuild node, the pair kernel with both half steps, the box sums), and
+    # the time the largest box would need on one SM at the measured per-SM rate (one box per block)
+    node_us = graph_node_us(local)
+    step_us = 1e3 * ms / a.steps
+    nmax = max(b.n for b in boxes)
+    persistent = {"graph_node_us": node_us, "nodes_per_step": 4, "step_us": step_us,
+                  "launch_share_of_step": 4 * node_us / step_us, "largest_box": nmax,
+                  "largest_box_on_one_sm_us": step_us * cu.attr(16, local) * nmax / n}  # 16: SM count
     cb = batch_cpu_baseline(boxes) if (rank == 0 and world == 1 and not a.no_cpu_baseline) else None
     if rank == 0:
         line = {
@@ -406,13 +415,40 @@ def run_batch(a, rank, world, local, pg):
                       "pressure_rel_err_max": float(dp.max()), "pressure_rel_err_median": float(np.median(dp)),
                       "one_at_a_time_fp64": {"value": seq, "unit": "molecule-updates/s",
                                              "sample": "16 boxes spread over the N range, md_ctx FP64, 100 steps each"},
-                      "speedup_vs_one_at_a_time_fp64": value / seq},
+                      "speedup_vs_one_at_a_time_fp64": value / seq,
+                      "persistent_launch_bound": persistent},
             "clocks": clocks,
             "e2e": {"value": world * n * a.steps / e2e_s, "unit": "molecule-updates/s",
                     "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps},
             "cpu_baseline": cb,
         }
         print(json.dumps(line))
+
+
+def graph_node_us(device: int, nodes: int = 400) -> float:
+    """Per-node cost of a replayed CUDA graph of `nodes` dependent one-block
+    kernels (torch capture; best of 20 replays), the launch cost that one
+    persistent kernel per chunk would save."""
+    import torch
+    x = torch.zeros(256, device=f"cuda:{device}")
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream(device=device)
+    with torch.cuda.stream(s):
+        x.add_(1.0)
+        torch.cuda.synchronize(device)
+        with torch.cuda.graph(g, stream=s):
+            for _ in range(nodes):
+                x.add_(1.0)
+    torch.cuda.synchronize(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = float("inf")
+    for _ in range(20):
+        e0.record()
+        g.replay()
+        e1.record()
+        torch.cuda.synchronize(device)
+        best = min(best, e0.elapsed_time(e1))
+    return best * 1e3 / nodes
 
 
 def _perturbed(ps, f: float):
@@ -674,9 +710,10 @@ def main():
         mps = psm.with_vacancies(psm.mixture(108_000, 18.0, 300.0, seed=4), 100_000, 18.0, 4)
         em = E.Engine(mps, 1.0, precision="mixed", skin=0.1, device=local)
         em.forces()
+        em.run(9.118e-5, 200, record=False)  # off the lattice, as the differentiation workload's snapshots
         ktm = em.time_kernels(5)
         em.close()
-        adj_mix = {"system": f"2CLJQ/1CLJD mixture, {mps.n:,} molecules, n=18 nm^-3, T=300 K, rc=1 nm",
+        adj_mix = {"system": f"2CLJQ/1CLJD mixture, {mps.n:,} molecules, n=18 nm^-3, T=300 K, rc=1 nm, after 200 steps",
                    "kernel_forward_ms": ktm.force_ms, "kernel_adjoint_ms": ktm.adjoint_ms,
                    "adjoint_over_forward": ktm.adjoint_ms / ktm.force_ms}
 

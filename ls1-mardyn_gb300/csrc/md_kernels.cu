@@ -1546,16 +1546,14 @@ static_assert(MD_SITE_VEC * MD_MAXS <= 32, "one lane per element loads the warp 
 // General multi-site molecules: all site pairs of every molecule pair inside
 // the molecule-centre cut-off (rc_lj for LJ centres, rc for the multipoles),
 // with calcFM folded in: F = sum f, M = sum d_site x f + multipole torques,
-// Vi = 1/2 sum m_d o f.  A warp serves the `mols` consecutive slots from
-// w * mols; with comp_sel >= 0 only the molecules of that component (one
-// launch per component keeps each launch on one component's site-pair code,
-// which the instruction caches then hold).  The per-molecule lane sums are
-// combined by a compensated warp sum, the energy and virial sums are
-// compensated (FP32) or plain (FP64) per lane over the warp's molecules.
+// Vi = 1/2 sum m_d o f.  One warp per molecule, 32 molecules per warp one
+// after another.  The per-molecule lane sums are combined by a compensated
+// warp sum, the energy and virial sums are compensated (FP32) or plain
+// (FP64) per lane over the warp's molecules.
 template <typename Real>
 __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOCKS : 3) k_force_ms(State S, const float4* xlf, const Real* sd, const Real* se,
                                                             int stride, const uint32_t* nbr, const int* nnb, int maxnb,
-                                                            double* partials, int pstride, int comp_sel, int mols) {
+                                                            double* partials, int pstride) {
     __shared__ Real soff[27][3];
     __shared__ uint32_t ring[MS_WARPS][128];
     __shared__ Real site_i[MS_WARPS][2][MD_MAXS][3];  // the warp's molecule: site offsets, orientations
@@ -1574,11 +1572,10 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
     int n_mol = 0, n_lj = 0, n_cc = 0, n_cd = 0, n_dd = 0, n_cq = 0, n_dq = 0, n_qq = 0;
     const Real epsRF = (Real)cP.epsRFInvrc3;
     const uint32_t sstride = MD_SITE_VEC * (uint32_t)stride;  // site records [slot][site][MD_SITE_VEC]; the host keeps cap * stride * MD_SITE_VEC < 2^32
-    for (int t = 0; t < mols; ++t) {
-        const int64_t i = w * mols + t;
+    for (int t = 0; t < MS_MOLS; ++t) {
+        const int64_t i = w * MS_MOLS + t;
         if (i >= S.n) break;  // warp-uniform
         const int ci = S.comp[i];
-        if (comp_sel >= 0 && ci != comp_sel) continue;  // another launch serves this molecule
         const CompDev& A = cP.comp[ci];
         Real pi[3];
         if (sizeof(Real) == 4) {
