@@ -2,16 +2,15 @@
 LeapfrogRMM + VCP1CLJRMM + PositionCellProcessorRMM +
 VelocityCellProcessorRMM).
 
-The reference's reduced memory mode does not compile with the g++ of this
-image (its ParticleIterator declares a constexpr defaulted copy constructor
-over MoleculeRMM, whose copy constructor is not constexpr), so there are no
-golden runs of it.  Its restatement in the oracle is pinned instead to the
-oracle's Leapfrog, which the golden runs of the reference pin: both
-integrators are the same Stoermer-Verlet scheme, so the positions, Upot and
-virial of every step agree to rounding, and the reduced mode's velocities are
-the Leapfrog velocities plus a half kick dt/(2m) F.  The engine is then
-checked against the oracle's reduced mode: FP64 to 1e-9 relative over 30
-steps, mixed precision to the NVE tolerances of the other parity tests.
+Pinned against the reference's own reduced-memory-mode runs
+(tests/golden/rmm_*.npz, written by tests/golden/make_rmm.py from the
+reference built with -DENABLE_REDUCED_MEMORY_MODE): the oracle's restatement
+to 1e-12 (records) and 1e-12 / 1e-11 (final positions / velocities), the
+engine in FP64 to 1e-9 and in mixed precision to the NVE tolerances of the
+other parity tests.  The oracle's reduced mode is also the oracle's Leapfrog
+with half-step velocities: both are the same Stoermer-Verlet scheme, so the
+positions, Upot and virial of every step agree to rounding, and the reduced
+mode's velocities are the Leapfrog velocities plus a half kick dt/(2m) F.
 """
 import numpy as np
 import pytest
@@ -32,6 +31,15 @@ def _lj_box(cells=6, rho=0.8, T=1.0, seed=3, mass=1.0):
         assert c.lj[0].eps == 1.0
         ps.v = ps.v / np.sqrt(mass)
     return ps
+
+
+def _golden(name):
+    import golden_io as G
+    ps, g = G.load(name)
+    return ps, g, ps.components[0].mass_inertia()[0]
+
+
+RMM_GOLDEN = ["rmm_lj500", "rmm_lj864_m17", "rmm_lj4000"]
 
 
 def _by_id(m):
@@ -61,6 +69,26 @@ def test_oracle_rmm_is_leapfrog_with_half_step_velocities(mass):
     assert np.isclose(rec_rm[-1, 2], (b["v"] ** 2).sum(), rtol=1e-13)
     assert np.all(rec_rm[:, 3] == 0.0)
     assert fo.site_pairs[0] > 0
+
+
+@pytest.mark.parametrize("name", RMM_GOLDEN)
+def test_oracle_rmm_matches_the_reference_rmm_run(name):
+    """The initial force pass with half the kick, then NVE steps, against the
+    reference's own reduced-memory-mode run of the same input."""
+    ps, g, m = _golden(name)
+    dt, n = float(g["dt"]), int(g["nsteps"])
+    o = Oracle(ps, g["rc"], threads=4)
+    fo = o.rmm_forces(0.5 * dt / m)
+    rec = o.rmm_run(dt, n)
+    st = g["steps"]
+    assert abs(fo.upot - st[0, 1]) <= 1e-12 * abs(st[0, 1])
+    assert abs(fo.virial - st[0, 2]) <= 1e-12 * abs(st[0, 2])
+    for col in range(3):  # Upot, virial, sum v^2 of every step
+        assert np.abs(rec[:, col] - st[1:, col + 1]).max() <= 1e-12 * np.abs(st[1:, col + 1]).max(), col
+    mo = _by_id(o.molecules())
+    np.testing.assert_array_equal(mo["ids"], g["out_ids"])
+    assert np.abs(mo["r"] - g["out_r"]).max() <= 1e-12
+    assert np.abs(mo["v"] - g["out_v"]).max() <= 1e-11
 
 
 def test_oracle_rmm_velocity_pass():
@@ -133,6 +161,33 @@ def test_rmm_run_matches_oracle(engine_mod, precision):
             assert np.abs(rec[:, col] - ref[:, col]).max() <= 2e-5 * np.abs(ref[:, col]).max(), col
         assert np.abs(m["r"] - mo["r"]).max() <= 1e-6
     assert np.all(rec[:, 3] == 0.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", RMM_GOLDEN)
+def test_rmm_run_matches_the_reference_rmm_run(engine_mod, name, precision):
+    """md_rmm_forces (half kick) + md_rmm_run against the reference's own
+    reduced-memory-mode run: FP64 1e-9; mixed precision 2e-5 on the records
+    and 1e-6 on the final positions, as the other NVE parity tests."""
+    ps, g, m = _golden(name)
+    dt, n = float(g["dt"]), int(g["nsteps"])
+    e = engine_mod.Engine(ps, g["rc"], precision=precision, skin=0.2)
+    fo = e.rmm_forces(0.5 * dt / m)
+    rec = e.rmm_run(dt, n)
+    got = _by_id(e.molecules())
+    e.close()
+    st = g["steps"]
+    tol = 1e-9 if precision == "fp64" else 2e-5
+    assert abs(fo.upot - st[0, 1]) <= tol * abs(st[0, 1])
+    for col in range(3):
+        assert np.abs(rec[:, col] - st[1:, col + 1]).max() <= tol * np.abs(st[1:, col + 1]).max(), col
+    np.testing.assert_array_equal(got["ids"], g["out_ids"])
+    if precision == "fp64":
+        assert np.abs(got["r"] - g["out_r"]).max() <= 1e-10
+        assert np.abs(got["v"] - g["out_v"]).max() <= 1e-9
+    else:
+        assert np.abs(got["r"] - g["out_r"]).max() <= 1e-6
 
 
 @pytest.mark.gpu
