@@ -1,0 +1,64 @@
+"""The reference's own mixed precision (its SPDP build: float pair
+arithmetic, double accumulation) as the yardstick of the engine's mixed
+precision.  Fixtures: tests/golden/spdp_*.npz (tests/golden/make_spdp.py),
+one force evaluation of the reference's SPDP build on the inputs of the
+periodic DPDP fixtures per_*.npz.
+
+CPU: the reference's SPDP pair counts equal its DPDP ones, and its errors
+against DPDP are those of FP32 pair arithmetic (force rms below 1e-5).
+GPU: on the same inputs the engine's mixed precision is at least as close
+to the reference's DPDP forces, torques, Upot and virial as the reference's
+own SPDP build (within a factor 1.5, plus a floor at FP64 rounding level)."""
+import numpy as np
+import pytest
+
+import golden_io as G
+
+CASES = ["lj500", "lj4000j", "lj864_rclj", "mix500", "slab"]
+
+
+def _rms(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum(1).mean() / (b ** 2).sum(1).mean()))
+
+
+def _spdp(case):
+    z = np.load(f"{G.GOLDEN}/spdp_{case}.npz")
+    ps, g = G.load(str(z["input"]))
+    np.testing.assert_array_equal(z["out_ids"], g["out_ids"])
+    return ps, g, z
+
+
+def _errors(F, M, upot, virial, g):
+    e = {"F": _rms(F, g["F"]), "upot": abs(upot - float(g["upot"])) / abs(float(g["upot"])),
+         "virial": abs(virial - float(g["virial"])) / abs(float(g["virial"]))}
+    if np.abs(g["M"]).max() > 0:
+        e["M"] = _rms(M, g["M"])
+    return e
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_reference_spdp_error_against_its_dpdp(case):
+    ps, g, z = _spdp(case)
+    np.testing.assert_array_equal(z["counts"], g["counts"])
+    e = _errors(z["F"], z["M"], float(z["upot"]), float(z["virial"]), g)
+    assert 0 < e["F"] < 1e-5, e
+    assert e["upot"] < 1e-5 and e["virial"] < 1e-5, e
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_engine_mixed_at_least_as_close_as_the_reference_spdp(case):
+    import build as eb
+    eb.build()
+    from ls1gb300 import engine as E
+    ps, g, z = _spdp(case)
+    ref = _errors(z["F"], z["M"], float(z["upot"]), float(z["virial"]), g)
+    e = E.Engine(ps, g["rc"], g["rc_lj"], precision="mixed")
+    fo = e.forces()
+    m = e.molecules()
+    e.close()
+    o = np.argsort(m["ids"])
+    got = _errors(m["F"][o], m["M"][o], fo.upot, fo.virial, g)
+    for k in ref:
+        floor = 1e-7 if k in ("F", "M") else 1e-9
+        assert got[k] <= 1.5 * ref[k] + floor, (k, got[k], ref[k])
