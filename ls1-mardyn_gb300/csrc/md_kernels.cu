@@ -1543,211 +1543,317 @@ static_assert(MD_SITE_VEC * MD_MAXS <= 32, "one lane per element loads the warp 
 #define MS_ADJ_MIN_BLOCKS 5  // FP32 adjoint kernel: the same (96 registers, no spills)
 #endif
 
+// Site signature of a component as the multi-site kernels read it (sites in
+// the order LJ centres, charges, dipoles, quadrupoles): SigDyn reads the
+// component's table at run time; SigFix<ID, NL, NC, ND, NQ> states component
+// ID's counts at compile time, so that the site-pair loops of a molecule pair
+// unroll into straight code with no kind dispatch.
+struct SigDyn {
+    const CompDev& c;
+    int id;
+    __device__ __forceinline__ int nlj() const { return c.nlj; }
+    __device__ __forceinline__ int nch() const { return c.nch; }
+    __device__ __forceinline__ int ndi() const { return c.ndi; }
+    __device__ __forceinline__ int nqu() const { return c.nqu; }
+    __device__ __forceinline__ int ns() const { return c.ns; }
+    __device__ __forceinline__ int ljoff() const { return c.ljoff; }
+    __device__ __forceinline__ int kind(int a) const { return c.kind[a]; }
+    __device__ __forceinline__ int comp() const { return id; }
+};
+template <int ID, int NL, int NC, int ND, int NQ>
+struct SigFix {
+    __device__ __forceinline__ static constexpr int nlj() { return NL; }
+    __device__ __forceinline__ static constexpr int nch() { return NC; }
+    __device__ __forceinline__ static constexpr int ndi() { return ND; }
+    __device__ __forceinline__ static constexpr int nqu() { return NQ; }
+    __device__ __forceinline__ static constexpr int ns() { return NL + NC + ND + NQ; }
+    __device__ __forceinline__ static int ljoff() { return cP.comp[ID].ljoff; }
+    __device__ __forceinline__ static constexpr int kind(int a) {
+        return a < NL ? SK_LJ : a < NL + NC ? SK_CHARGE : a < NL + NC + ND ? SK_DIPOLE : SK_QUAD;
+    }
+    __device__ __forceinline__ static constexpr int comp() { return ID; }
+};
+
+// Pair counts by kind of one warp (molecule pairs, LJ, C-C, C-D, D-D, C-Q, D-Q, Q-Q).
+struct MsCounts {
+    int mol = 0, lj = 0, cc = 0, cd = 0, dd = 0, cq = 0, dq = 0, qq = 0;
+};
+
+// One molecule pair: the LJ x LJ site pairs, then each electrostatic site of
+// the home molecule (A) against the charges, dipoles and quadrupoles of the
+// neighbour (B), one body per kind pair.  The home-site forces are summed per
+// site before its lever-arm torque; the virial of the molecule pair is
+// m_d o (sum of its site forces).  fp, mp: force and torque on the home
+// molecule; u6p, uxp, rfp: its LJ (times 6), multipole and reaction-field
+// energies.
+template <typename Real, class SA, class SB>
+__device__ __forceinline__ void ms_molpair(const SA& A, const SB& B, const Real (*da_t)[3], const Real (*ea_t)[3],
+                                           const Real* sd, const Real* se, uint32_t jb, const Real* md, int fl,
+                                           bool macro, Real epsRF, Real* fp, Real* mp, Real& u6p, Real& uxp, Real& rfp,
+                                           MsCounts& n) {
+    if (fl & 1) {
+        const int nlb = B.nlj();
+        for (int a = 0; a < A.nlj(); ++a) {
+            const Real* da = da_t[a];
+            const int row = (A.ljoff() + a) * cP.nlj + B.ljoff();
+            Real fa[3] = {0, 0, 0};
+            for (int b = 0; b < nlb; ++b) {
+                Real db[3];
+                site_rec<Real>(sd + jb + MD_SITE_VEC * (uint32_t)b, db);
+                const Real ds[3] = {md[0] + (da[0] - db[0]), md[1] + (da[1] - db[1]), md[2] + (da[2] - db[2])};
+                const Real s2r = ds[0] * ds[0] + (ds[1] * ds[1] + ds[2] * ds[2]);
+                Real f[3], Vd[3], u;
+                lj_pair<Real>(ds, md, s2r, PTab<Real>::eps24(cP, row + b), PTab<Real>::sig2(cP, row + b),
+                              PTab<Real>::shift6(cP, row + b), f, Vd, u);
+                fa[0] += f[0]; fa[1] += f[1]; fa[2] += f[2];
+                u6p += u;
+            }
+            mp[0] += da[1] * fa[2] - da[2] * fa[1];
+            mp[1] += da[2] * fa[0] - da[0] * fa[2];
+            mp[2] += da[0] * fa[1] - da[1] * fa[0];
+            fp[0] += fa[0]; fp[1] += fa[1]; fp[2] += fa[2];
+        }
+        if (macro) n.lj += A.nlj() * nlb;
+    }
+    if (fl & 2) {
+        const int b0 = B.nlj(), b1 = b0 + B.nch(), b2 = b1 + B.ndi(), b3 = B.ns();
+        for (int a = A.nlj(); a < A.ns(); ++a) {
+            const int ka = A.kind(a);  // warp-uniform: A is the warp's molecule
+            const Real* da = da_t[a];
+            const Real* ea = ea_t[a];
+            const Real pa = PTab<Real>::p(cP, A.comp(), a);
+            Real fa[3] = {0, 0, 0}, ta[3] = {0, 0, 0};
+            auto site_j = [&](int b, Real* ds, Real* eb) {
+                const uint32_t ob = jb + MD_SITE_VEC * (uint32_t)b;
+                Real db[3];
+                site_rec<Real>(sd + ob, db);
+                site_rec<Real>(se + ob, eb);
+                for (int c = 0; c < 3; ++c) ds[c] = md[c] + (da[c] - db[c]);
+            };
+            Real ds[3], eb[3], f[3], T[3], Tj[3], u, urf;
+            if (ka == SK_CHARGE) {
+                for (int b = b0; b < b1; ++b) {
+                    site_j(b, ds, eb);
+                    cc_body<Real>(ds, pa, PTab<Real>::p(cP, B.comp(), b), f, u);
+                    for (int c = 0; c < 3; ++c) fa[c] += f[c];
+                    uxp += u;
+                }
+                for (int b = b1; b < b2; ++b) {
+                    site_j(b, ds, eb);
+                    cd_body<Real>(ds, pa, eb, PTab<Real>::p(cP, B.comp(), b), f, Tj, u);
+                    for (int c = 0; c < 3; ++c) fa[c] += f[c];
+                    uxp += u;
+                }
+                for (int b = b2; b < b3; ++b) {
+                    site_j(b, ds, eb);
+                    cq_body<Real>(ds, pa, eb, PTab<Real>::p(cP, B.comp(), b), f, Tj, u);
+                    for (int c = 0; c < 3; ++c) fa[c] += f[c];
+                    uxp += u;
+                }
+                if (macro) { n.cc += B.nch(); n.cd += B.ndi(); n.cq += B.nqu(); }
+            } else if (ka == SK_DIPOLE) {
+                for (int b = b0; b < b1; ++b) {
+                    site_j(b, ds, eb);
+                    const Real nd[3] = {-ds[0], -ds[1], -ds[2]};
+                    cd_body<Real>(nd, PTab<Real>::p(cP, B.comp(), b), ea, pa, f, T, u);
+                    for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
+                    uxp += u;
+                }
+                for (int b = b1; b < b2; ++b) {
+                    site_j(b, ds, eb);
+                    dd_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, B.comp(), b), epsRF, f, T, u, urf);
+                    for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
+                    uxp += u;
+                    rfp += urf;
+                }
+                for (int b = b2; b < b3; ++b) {
+                    site_j(b, ds, eb);
+                    dq_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, B.comp(), b), f, T, Tj, u);
+                    for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
+                    uxp += u;
+                }
+                if (macro) { n.cd += B.nch(); n.dd += B.ndi(); n.dq += B.nqu(); }
+            } else {
+                for (int b = b0; b < b1; ++b) {
+                    site_j(b, ds, eb);
+                    const Real nd[3] = {-ds[0], -ds[1], -ds[2]};
+                    cq_body<Real>(nd, PTab<Real>::p(cP, B.comp(), b), ea, pa, f, T, u);
+                    for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
+                    uxp += u;
+                }
+                for (int b = b1; b < b2; ++b) {
+                    site_j(b, ds, eb);
+                    const Real nd[3] = {-ds[0], -ds[1], -ds[2]};
+                    dq_body<Real>(nd, eb, PTab<Real>::p(cP, B.comp(), b), ea, pa, f, Tj, T, u);
+                    for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
+                    uxp += u;
+                }
+                for (int b = b2; b < b3; ++b) {
+                    site_j(b, ds, eb);
+                    qq_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, B.comp(), b), f, T, Tj, u);
+                    for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
+                    uxp += u;
+                }
+                if (macro) { n.cq += B.nch(); n.dq += B.ndi(); n.qq += B.nqu(); }
+            }
+            // torque of the site force about the centre plus the multipole torque
+            mp[0] += (da[1] * fa[2] - da[2] * fa[1]) + ta[0];
+            mp[1] += (da[2] * fa[0] - da[0] * fa[2]) + ta[1];
+            mp[2] += (da[0] * fa[1] - da[1] * fa[0]) + ta[2];
+            fp[0] += fa[0]; fp[1] += fa[1]; fp[2] += fa[2];
+        }
+    }
+}
+
+// Per-warp state of the multi-site force kernels.
+template <typename Real>
+struct MsWarp {
+    typename Acc<Real>::type u6, ux, vir, rf;
+    MsCounts n;
+};
+
+// Molecule i (the warp's, of signature A): its site records into the warp's
+// shared rows, its candidate row walked with the whole warp, every
+// in-cut-off neighbour handed to `pair(A, neighbour component, ...)`, and
+// the per-molecule sums stored.  The per-lane sums of the molecule are plain
+// (a lane adds two or three molecule pairs) and combined by a compensated
+// warp sum; the energy and virial sums are compensated (FP32) or plain
+// (FP64) per lane over the warp's molecules.
+template <typename Real, class SA, class Pair>
+__device__ __forceinline__ void ms_molecule(const State& S, const float4* xlf, const Real* sd, const Real* se,
+                                            uint32_t sstride, const uint32_t* nbr, const int* nnb, int maxnb,
+                                            const Real (*soff)[3], uint32_t* ring, Real (*site_i)[MD_MAXS][3],
+                                            int lane, int64_t i, const SA& A, Real epsRF, MsWarp<Real>& W, Pair pair) {
+    Real pi[3];
+    if (sizeof(Real) == 4) {
+        const float4 p = xlf[i];
+        pi[0] = p.x; pi[1] = p.y; pi[2] = p.z;
+    } else {
+        pi[0] = S.rx[i]; pi[1] = S.ry[i]; pi[2] = S.rz[i];
+    }
+    __syncwarp();
+    if (lane < MD_SITE_VEC * A.ns() && lane % MD_SITE_VEC < 3) {  // MD_SITE_VEC * MD_MAXS = 32 lanes
+        site_i[0][lane / MD_SITE_VEC][lane % MD_SITE_VEC] = sd[(uint32_t)i * sstride + lane];
+        site_i[1][lane / MD_SITE_VEC][lane % MD_SITE_VEC] = se[(uint32_t)i * sstride + lane];
+    }
+    __syncwarp();
+    Real F[3] = {0, 0, 0}, M[3] = {0, 0, 0}, V[3] = {0, 0, 0};
+    auto body = [&](uint32_t e, int fl, const Real* md) {
+        const uint32_t j = e & MD_INDEX_MASK;
+        const bool macro = (int64_t)j > i;
+        Real fp[3] = {0, 0, 0}, mp[3] = {0, 0, 0};
+        Real u6p = 0, uxp = 0, rfp = 0;
+        pair(S.comp[j], site_i[0], site_i[1], j * sstride, md, fl, macro, epsRF, fp, mp, u6p, uxp, rfp, W.n);
+        const Real vp[3] = {md[0] * fp[0], md[1] * fp[1], md[2] * fp[2]};
+        for (int c = 0; c < 3; ++c) { F[c] += fp[c]; M[c] += mp[c]; V[c] += vp[c]; }
+        if (macro) {
+            if (fl & 2) W.n.mol += 1;
+            W.u6.add(u6p);
+            W.ux.add(uxp);
+            W.rf.add(rfp);
+            W.vir.add(vp[0] + vp[1] + vp[2]);
+        }
+    };
+    ms_walk_row<Real>(S, xlf, soff, pi, i, nbr + (size_t)i * maxnb, nnb[i], ring, lane, body);
+    const double fx = warp_total_plain(F[0]), fy = warp_total_plain(F[1]), fz = warp_total_plain(F[2]);
+    const double mx = warp_total_plain(M[0]), my = warp_total_plain(M[1]), mz = warp_total_plain(M[2]);
+    const double vx = warp_total_plain(V[0], 0.5f), vy = warp_total_plain(V[1], 0.5f), vz = warp_total_plain(V[2], 0.5f);
+    if (lane == 0) {
+        S.Fx[i] = fx; S.Fy[i] = fy; S.Fz[i] = fz;
+        S.Mx[i] = mx; S.My[i] = my; S.Mz[i] = mz;
+        S.Vx[i] = vx; S.Vy[i] = vy; S.Vz[i] = vz;
+    }
+}
+
+template <typename Real>
+__device__ __forceinline__ void ms_store_partials(double* partials, int pstride, const MsWarp<Real>& W) {
+    warp_partial_acc(partials, pstride, 0, W.u6, 1.f);
+    warp_partial_acc(partials, pstride, 1, W.ux, 1.f);
+    warp_partial_acc(partials, pstride, 2, W.vir, 1.f);
+    warp_partial_acc(partials, pstride, 3, W.rf, -1.f);
+    const int cnts[8] = {W.n.mol, W.n.lj, W.n.cc, W.n.cd, W.n.dd, W.n.cq, W.n.dq, W.n.qq};
+#pragma unroll
+    for (int sl = 0; sl < 8; ++sl) warp_partial_count(partials, pstride, 4 + sl, (float)cnts[sl]);
+}
+
+// The shared-memory setup common to both multi-site kernels.
+#define MS_SHARED_SETUP                                                                  \
+    __shared__ Real soff[27][3];                                                         \
+    __shared__ uint32_t ring[MS_WARPS][128];                                             \
+    __shared__ Real site_i[MS_WARPS][2][MD_MAXS][3];                                     \
+    if (threadIdx.x < 27) {                                                              \
+        int t = threadIdx.x;                                                             \
+        soff[t][0] = (Real)((t % 3 - 1) * cP.lside[0]);                                  \
+        soff[t][1] = (Real)(((t / 3) % 3 - 1) * cP.lside[1]);                            \
+        soff[t][2] = (Real)((t / 9 - 1) * cP.lside[2]);                                  \
+    }                                                                                    \
+    __syncthreads();                                                                     \
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;                            \
+    const int64_t w = (int64_t)blockIdx.x * MS_WARPS + wl;                               \
+    MsWarp<Real> W;                                                                      \
+    W.u6.init(); W.ux.init(); W.vir.init(); W.rf.init();                                 \
+    const Real epsRF = (Real)cP.epsRFInvrc3;                                             \
+    /* site records [slot][site][MD_SITE_VEC]; the host keeps cap * stride * MD_SITE_VEC < 2^32 */ \
+    const uint32_t sstride = MD_SITE_VEC * (uint32_t)stride;
+
 // General multi-site molecules: all site pairs of every molecule pair inside
 // the molecule-centre cut-off (rc_lj for LJ centres, rc for the multipoles),
 // with calcFM folded in: F = sum f, M = sum d_site x f + multipole torques,
 // Vi = 1/2 sum m_d o f.  One warp per molecule, 32 molecules per warp one
-// after another.  The per-molecule lane sums are combined by a compensated
-// warp sum, the energy and virial sums are compensated (FP32) or plain
-// (FP64) per lane over the warp's molecules.
+// after another; component signatures read at run time.
 template <typename Real>
 __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOCKS : 3) k_force_ms(State S, const float4* xlf, const Real* sd, const Real* se,
                                                             int stride, const uint32_t* nbr, const int* nnb, int maxnb,
                                                             double* partials, int pstride) {
-    __shared__ Real soff[27][3];
-    __shared__ uint32_t ring[MS_WARPS][128];
-    __shared__ Real site_i[MS_WARPS][2][MD_MAXS][3];  // the warp's molecule: site offsets, orientations
-    if (threadIdx.x < 27) {
-        int t = threadIdx.x;
-        soff[t][0] = (Real)((t % 3 - 1) * cP.lside[0]);
-        soff[t][1] = (Real)(((t / 3) % 3 - 1) * cP.lside[1]);
-        soff[t][2] = (Real)((t / 9 - 1) * cP.lside[2]);
-    }
-    __syncthreads();
-    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t w = (int64_t)blockIdx.x * MS_WARPS + wl;
-    typename Acc<Real>::type u6, ux, vir, rf;
-    u6.init(); ux.init(); vir.init(); rf.init();
-    // pair counts by kind (molecule pairs, LJ, C-C, C-D, D-D, C-Q, D-Q, Q-Q), in registers
-    int n_mol = 0, n_lj = 0, n_cc = 0, n_cd = 0, n_dd = 0, n_cq = 0, n_dq = 0, n_qq = 0;
-    const Real epsRF = (Real)cP.epsRFInvrc3;
-    const uint32_t sstride = MD_SITE_VEC * (uint32_t)stride;  // site records [slot][site][MD_SITE_VEC]; the host keeps cap * stride * MD_SITE_VEC < 2^32
+    MS_SHARED_SETUP
     for (int t = 0; t < MS_MOLS; ++t) {
         const int64_t i = w * MS_MOLS + t;
         if (i >= S.n) break;  // warp-uniform
         const int ci = S.comp[i];
-        const CompDev& A = cP.comp[ci];
-        Real pi[3];
-        if (sizeof(Real) == 4) {
-            const float4 p = xlf[i];
-            pi[0] = p.x; pi[1] = p.y; pi[2] = p.z;
-        } else {
-            pi[0] = S.rx[i]; pi[1] = S.ry[i]; pi[2] = S.rz[i];
-        }
-        __syncwarp();
-        if (lane < MD_SITE_VEC * A.ns && lane % MD_SITE_VEC < 3) {  // MD_SITE_VEC * MD_MAXS = 32 lanes
-            site_i[wl][0][lane / MD_SITE_VEC][lane % MD_SITE_VEC] = sd[(uint32_t)i * sstride + lane];
-            site_i[wl][1][lane / MD_SITE_VEC][lane % MD_SITE_VEC] = se[(uint32_t)i * sstride + lane];
-        }
-        __syncwarp();
-        // per-lane sums of this molecule's force, torque and virial: a lane adds two or three molecule pairs,
-        // so plain sums; the lanes are combined by a compensated warp sum
-        Real F[3] = {0, 0, 0}, M[3] = {0, 0, 0}, V[3] = {0, 0, 0};
-        // One molecule pair: the site pairs in blocks by kind (LJ x LJ, then each
-        // electrostatic site of i against the charges, dipoles and quadrupoles
-        // of j), so that every block has one body and warp-uniform trip counts
-        // where the neighbours share a component.  The i-site forces are summed
-        // per site before its lever-arm torque; the virial of the molecule
-        // pair is m_d o (sum of its site forces).
-        auto body = [&](uint32_t e, int fl, const Real* md) {
-            const uint32_t j = e & MD_INDEX_MASK;
-            const int cj = S.comp[j];
-            const CompDev& B = cP.comp[cj];
-            const bool macro = (int64_t)j > i;
-            const uint32_t jb = j * sstride;
-            Real fp[3] = {0, 0, 0}, mp[3] = {0, 0, 0};
-            Real u6p = 0, uxp = 0, rfp = 0;
-            if (fl & 1) {
-                const int nlb = B.nlj;
-                for (int a = 0; a < A.nlj; ++a) {
-                    const Real* da = site_i[wl][0][a];
-                    const int row = (A.ljoff + a) * cP.nlj + B.ljoff;
-                    Real fa[3] = {0, 0, 0};
-                    for (int b = 0; b < nlb; ++b) {
-                        Real db[3];
-                        site_rec<Real>(sd + jb + MD_SITE_VEC * (uint32_t)b, db);
-                        const Real ds[3] = {md[0] + (da[0] - db[0]), md[1] + (da[1] - db[1]), md[2] + (da[2] - db[2])};
-                        const Real s2r = ds[0] * ds[0] + (ds[1] * ds[1] + ds[2] * ds[2]);
-                        Real f[3], Vd[3], u;
-                        lj_pair<Real>(ds, md, s2r, PTab<Real>::eps24(cP, row + b), PTab<Real>::sig2(cP, row + b),
-                                      PTab<Real>::shift6(cP, row + b), f, Vd, u);
-                        fa[0] += f[0]; fa[1] += f[1]; fa[2] += f[2];
-                        u6p += u;
-                    }
-                    mp[0] += da[1] * fa[2] - da[2] * fa[1];
-                    mp[1] += da[2] * fa[0] - da[0] * fa[2];
-                    mp[2] += da[0] * fa[1] - da[1] * fa[0];
-                    fp[0] += fa[0]; fp[1] += fa[1]; fp[2] += fa[2];
-                }
-                if (macro) n_lj += A.nlj * nlb;
-            }
-            if (fl & 2) {
-                const int b0 = B.nlj, b1 = b0 + B.nch, b2 = b1 + B.ndi, b3 = B.ns;
-                for (int a = A.nlj; a < A.ns; ++a) {
-                    const int ka = A.kind[a];  // warp-uniform: i is the warp's molecule
-                    const Real* da = site_i[wl][0][a];
-                    const Real* ea = site_i[wl][1][a];
-                    const Real pa = PTab<Real>::p(cP, ci, a);
-                    Real fa[3] = {0, 0, 0}, ta[3] = {0, 0, 0};
-                    auto site_j = [&](int b, Real* ds, Real* eb) {
-                        const uint32_t ob = jb + MD_SITE_VEC * (uint32_t)b;
-                        Real db[3];
-                        site_rec<Real>(sd + ob, db);
-                        site_rec<Real>(se + ob, eb);
-                        for (int c = 0; c < 3; ++c) ds[c] = md[c] + (da[c] - db[c]);
-                    };
-                    Real ds[3], eb[3], f[3], T[3], Tj[3], u, urf;
-                    if (ka == SK_CHARGE) {
-                        for (int b = b0; b < b1; ++b) {
-                            site_j(b, ds, eb);
-                            cc_body<Real>(ds, pa, PTab<Real>::p(cP, cj, b), f, u);
-                            for (int c = 0; c < 3; ++c) fa[c] += f[c];
-                            uxp += u;
-                        }
-                        for (int b = b1; b < b2; ++b) {
-                            site_j(b, ds, eb);
-                            cd_body<Real>(ds, pa, eb, PTab<Real>::p(cP, cj, b), f, Tj, u);
-                            for (int c = 0; c < 3; ++c) fa[c] += f[c];
-                            uxp += u;
-                        }
-                        for (int b = b2; b < b3; ++b) {
-                            site_j(b, ds, eb);
-                            cq_body<Real>(ds, pa, eb, PTab<Real>::p(cP, cj, b), f, Tj, u);
-                            for (int c = 0; c < 3; ++c) fa[c] += f[c];
-                            uxp += u;
-                        }
-                        if (macro) { n_cc += B.nch; n_cd += B.ndi; n_cq += B.nqu; }
-                    } else if (ka == SK_DIPOLE) {
-                        for (int b = b0; b < b1; ++b) {
-                            site_j(b, ds, eb);
-                            const Real nd[3] = {-ds[0], -ds[1], -ds[2]};
-                            cd_body<Real>(nd, PTab<Real>::p(cP, cj, b), ea, pa, f, T, u);
-                            for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
-                            uxp += u;
-                        }
-                        for (int b = b1; b < b2; ++b) {
-                            site_j(b, ds, eb);
-                            dd_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, cj, b), epsRF, f, T, u, urf);
-                            for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
-                            uxp += u;
-                            rfp += urf;
-                        }
-                        for (int b = b2; b < b3; ++b) {
-                            site_j(b, ds, eb);
-                            dq_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, cj, b), f, T, Tj, u);
-                            for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
-                            uxp += u;
-                        }
-                        if (macro) { n_cd += B.nch; n_dd += B.ndi; n_dq += B.nqu; }
-                    } else {
-                        for (int b = b0; b < b1; ++b) {
-                            site_j(b, ds, eb);
-                            const Real nd[3] = {-ds[0], -ds[1], -ds[2]};
-                            cq_body<Real>(nd, PTab<Real>::p(cP, cj, b), ea, pa, f, T, u);
-                            for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
-                            uxp += u;
-                        }
-                        for (int b = b1; b < b2; ++b) {
-                            site_j(b, ds, eb);
-                            const Real nd[3] = {-ds[0], -ds[1], -ds[2]};
-                            dq_body<Real>(nd, eb, PTab<Real>::p(cP, cj, b), ea, pa, f, Tj, T, u);
-                            for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
-                            uxp += u;
-                        }
-                        for (int b = b2; b < b3; ++b) {
-                            site_j(b, ds, eb);
-                            qq_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, cj, b), f, T, Tj, u);
-                            for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
-                            uxp += u;
-                        }
-                        if (macro) { n_cq += B.nch; n_dq += B.ndi; n_qq += B.nqu; }
-                    }
-                    // torque of the site force about the centre plus the multipole torque
-                    mp[0] += (da[1] * fa[2] - da[2] * fa[1]) + ta[0];
-                    mp[1] += (da[2] * fa[0] - da[0] * fa[2]) + ta[1];
-                    mp[2] += (da[0] * fa[1] - da[1] * fa[0]) + ta[2];
-                    fp[0] += fa[0]; fp[1] += fa[1]; fp[2] += fa[2];
-                }
-            }
-            const Real vp[3] = {md[0] * fp[0], md[1] * fp[1], md[2] * fp[2]};
-            for (int c = 0; c < 3; ++c) { F[c] += fp[c]; M[c] += mp[c]; V[c] += vp[c]; }
-            if (macro) {
-                if (fl & 2) n_mol += 1;
-                u6.add(u6p);
-                ux.add(uxp);
-                rf.add(rfp);
-                vir.add(vp[0] + vp[1] + vp[2]);
-            }
+        const SigDyn A{cP.comp[ci], ci};
+        auto pair = [&](int cj, const Real (*da_t)[3], const Real (*ea_t)[3], uint32_t jb, const Real* md, int fl,
+                        bool macro, Real eps, Real* fp, Real* mp, Real& u6p, Real& uxp, Real& rfp, MsCounts& n) {
+            const SigDyn B{cP.comp[cj], cj};
+            ms_molpair<Real>(A, B, da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, u6p, uxp, rfp, n);
         };
-        ms_walk_row<Real>(S, xlf, soff, pi, i, nbr + (size_t)i * maxnb, nnb[i], ring[wl], lane, body);
-        const double fx = warp_total_plain(F[0]), fy = warp_total_plain(F[1]), fz = warp_total_plain(F[2]);
-        const double mx = warp_total_plain(M[0]), my = warp_total_plain(M[1]), mz = warp_total_plain(M[2]);
-        const double vx = warp_total_plain(V[0], 0.5f), vy = warp_total_plain(V[1], 0.5f),
-                     vz = warp_total_plain(V[2], 0.5f);
-        if (lane == 0) {
-            S.Fx[i] = fx; S.Fy[i] = fy; S.Fz[i] = fz;
-            S.Mx[i] = mx; S.My[i] = my; S.Mz[i] = mz;
-            S.Vx[i] = vx; S.Vy[i] = vy; S.Vz[i] = vz;
-        }
+        ms_molecule<Real>(S, xlf, sd, se, sstride, nbr, nnb, maxnb, soff, ring[wl], site_i[wl], lane, i, A, epsRF, W,
+                          pair);
     }
-    warp_partial_acc(partials, pstride, 0, u6, 1.f);
-    warp_partial_acc(partials, pstride, 1, ux, 1.f);
-    warp_partial_acc(partials, pstride, 2, vir, 1.f);
-    warp_partial_acc(partials, pstride, 3, rf, -1.f);
-    const int cnts[8] = {n_mol, n_lj, n_cc, n_cd, n_dd, n_cq, n_dq, n_qq};
-#pragma unroll
-    for (int sl = 0; sl < 8; ++sl) warp_partial_count(partials, pstride, 4 + sl, (float)cnts[sl]);
+    ms_store_partials<Real>(partials, pstride, W);
 }
+
+// The same for a two-component system whose component signatures are S0 and
+// S1 at compile time (chosen at setup when the components match a compiled
+// pair of signatures): every molecule pair's site loops are straight code.
+template <typename Real, class S0, class S1>
+__global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOCKS : 3) k_force_ms2(State S, const float4* xlf, const Real* sd, const Real* se,
+                                                             int stride, const uint32_t* nbr, const int* nnb, int maxnb,
+                                                             double* partials, int pstride) {
+    MS_SHARED_SETUP
+    for (int t = 0; t < MS_MOLS; ++t) {
+        const int64_t i = w * MS_MOLS + t;
+        if (i >= S.n) break;  // warp-uniform
+        auto run = [&](auto A) {
+            auto pair = [&](int cj, const Real (*da_t)[3], const Real (*ea_t)[3], uint32_t jb, const Real* md, int fl,
+                            bool macro, Real eps, Real* fp, Real* mp, Real& u6p, Real& uxp, Real& rfp, MsCounts& n) {
+                if (cj == 0)
+                    ms_molpair<Real>(A, S0(), da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, u6p, uxp, rfp, n);
+                else
+                    ms_molpair<Real>(A, S1(), da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, u6p, uxp, rfp, n);
+            };
+            ms_molecule<Real>(S, xlf, sd, se, sstride, nbr, nnb, maxnb, soff, ring[wl], site_i[wl], lane, i, A, epsRF,
+                              W, pair);
+        };
+        if (S.comp[i] == 0) run(S0());
+        else run(S1());
+    }
+    ms_store_partials<Real>(partials, pstride, W);
+}
+
+// Signatures the two-component kernel is compiled for: the 2CLJQ + 1CLJD
+// mixture (two LJ centres and a quadrupole; one LJ centre and a dipole).
+typedef SigFix<0, 2, 0, 0, 1> SigMixA;
+typedef SigFix<1, 1, 0, 1, 0> SigMixB;
 
 // ------------------------------------------------------------------ integration
 // FullMolecule::upd_preF; afterwards the FP32 local coordinates and the
