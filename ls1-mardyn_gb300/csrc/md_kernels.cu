@@ -1545,9 +1545,11 @@ static_assert(MD_SITE_VEC * MD_MAXS <= 32, "one lane per element loads the warp 
 
 // Site signature of a component as the multi-site kernels read it (sites in
 // the order LJ centres, charges, dipoles, quadrupoles): SigDyn reads the
-// component's table at run time; SigFix<ID, NL, NC, ND, NQ> states component
-// ID's counts at compile time, so that the site-pair loops of a molecule pair
-// unroll into straight code with no kind dispatch.
+// component's table at run time; SigFix<ID, NL, NC, ND, NQ, LJOFF, LJTOT>
+// states component ID's counts, the global index of its first LJ centre and
+// the system's number of LJ centres at compile time, so that the site-pair
+// loops of a molecule pair unroll into straight code with no kind dispatch
+// and constant parameter-table offsets.
 struct SigDyn {
     const CompDev& c;
     int id;
@@ -1557,21 +1559,38 @@ struct SigDyn {
     __device__ __forceinline__ int nqu() const { return c.nqu; }
     __device__ __forceinline__ int ns() const { return c.ns; }
     __device__ __forceinline__ int ljoff() const { return c.ljoff; }
+    __device__ __forceinline__ int ljtot() const { return cP.nlj; }
     __device__ __forceinline__ int kind(int a) const { return c.kind[a]; }
     __device__ __forceinline__ int comp() const { return id; }
 };
-template <int ID, int NL, int NC, int ND, int NQ>
+template <int ID, int NL, int NC, int ND, int NQ, int LJOFF, int LJTOT>
 struct SigFix {
     __device__ __forceinline__ static constexpr int nlj() { return NL; }
     __device__ __forceinline__ static constexpr int nch() { return NC; }
     __device__ __forceinline__ static constexpr int ndi() { return ND; }
     __device__ __forceinline__ static constexpr int nqu() { return NQ; }
     __device__ __forceinline__ static constexpr int ns() { return NL + NC + ND + NQ; }
-    __device__ __forceinline__ static int ljoff() { return cP.comp[ID].ljoff; }
+    __device__ __forceinline__ static constexpr int ljoff() { return LJOFF; }
+    __device__ __forceinline__ static constexpr int ljtot() { return LJTOT; }
     __device__ __forceinline__ static constexpr int kind(int a) {
         return a < NL ? SK_LJ : a < NL + NC ? SK_CHARGE : a < NL + NC + ND ? SK_DIPOLE : SK_QUAD;
     }
     __device__ __forceinline__ static constexpr int comp() { return ID; }
+};
+
+// Signature dispatch by component index: DispDyn hands `f` the run-time
+// signature; DispFix2<S0, S1> the compile-time one of a two-component system.
+struct DispDyn {
+    template <class F>
+    __device__ __forceinline__ static void run(int c, F f) { f(SigDyn{cP.comp[c], c}); }
+};
+template <class S0, class S1>
+struct DispFix2 {
+    template <class F>
+    __device__ __forceinline__ static void run(int c, F f) {
+        if (c == 0) f(S0());
+        else f(S1());
+    }
 };
 
 // Pair counts by kind of one warp (molecule pairs, LJ, C-C, C-D, D-D, C-Q, D-Q, Q-Q).
@@ -1595,7 +1614,7 @@ __device__ __forceinline__ void ms_molpair(const SA& A, const SB& B, const Real 
         const int nlb = B.nlj();
         for (int a = 0; a < A.nlj(); ++a) {
             const Real* da = da_t[a];
-            const int row = (A.ljoff() + a) * cP.nlj + B.ljoff();
+            const int row = (A.ljoff() + a) * A.ljtot() + B.ljoff();
             Real fa[3] = {0, 0, 0};
             for (int b = 0; b < nlb; ++b) {
                 Real db[3];
@@ -1852,8 +1871,8 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
 
 // Signatures the two-component kernel is compiled for: the 2CLJQ + 1CLJD
 // mixture (two LJ centres and a quadrupole; one LJ centre and a dipole).
-typedef SigFix<0, 2, 0, 0, 1> SigMixA;
-typedef SigFix<1, 1, 0, 1, 0> SigMixB;
+typedef SigFix<0, 2, 0, 0, 1, 0, 3> SigMixA;
+typedef SigFix<1, 1, 0, 1, 0, 2, 3> SigMixB;
 
 // ------------------------------------------------------------------ integration
 // FullMolecule::upd_preF; afterwards the FP32 local coordinates and the
