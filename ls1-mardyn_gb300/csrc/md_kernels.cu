@@ -1542,6 +1542,7 @@ static_assert(MD_SITE_VEC * MD_MAXS <= 32, "one lane per element loads the warp 
 #ifndef MS_ADJ_MIN_BLOCKS
 #define MS_ADJ_MIN_BLOCKS 5  // FP32 adjoint kernel: the same (96 registers, no spills)
 #endif
+#define MS_ADJ_MIN_MOLS 8  // fewest molecules per warp of the multi-site adjoint
 
 // Site signature of a component as the multi-site kernels read it (sites in
 // the order LJ centres, charges, dipoles, quadrupoles): SigDyn reads the
