@@ -1732,18 +1732,18 @@ struct MsWarp {
     MsCounts n;
 };
 
-// Molecule i (the warp's, of signature A): its site records into the warp's
+// Molecule i (the warp's, with ns sites): its site records into the warp's
 // shared rows, its candidate row walked with the whole warp, every
-// in-cut-off neighbour handed to `pair(A, neighbour component, ...)`, and
+// in-cut-off neighbour handed to `pair(neighbour component, ...)`, and
 // the per-molecule sums stored.  The per-lane sums of the molecule are plain
 // (a lane adds two or three molecule pairs) and combined by a compensated
 // warp sum; the energy and virial sums are compensated (FP32) or plain
 // (FP64) per lane over the warp's molecules.
-template <typename Real, class SA, class Pair>
+template <typename Real, class Pair>
 __device__ __forceinline__ void ms_molecule(const State& S, const float4* xlf, const Real* sd, const Real* se,
                                             uint32_t sstride, const uint32_t* nbr, const int* nnb, int maxnb,
                                             const Real (*soff)[3], uint32_t* ring, Real (*site_i)[MD_MAXS][3],
-                                            int lane, int64_t i, const SA& A, Real epsRF, MsWarp<Real>& W, Pair pair) {
+                                            int lane, int64_t i, int ns, Real epsRF, MsWarp<Real>& W, Pair pair) {
     Real pi[3];
     if (sizeof(Real) == 4) {
         const float4 p = xlf[i];
@@ -1752,7 +1752,7 @@ __device__ __forceinline__ void ms_molecule(const State& S, const float4* xlf, c
         pi[0] = S.rx[i]; pi[1] = S.ry[i]; pi[2] = S.rz[i];
     }
     __syncwarp();
-    if (lane < MD_SITE_VEC * A.ns() && lane % MD_SITE_VEC < 3) {  // MD_SITE_VEC * MD_MAXS = 32 lanes
+    if (lane < MD_SITE_VEC * ns && lane % MD_SITE_VEC < 3) {  // MD_SITE_VEC * MD_MAXS = 32 lanes
         site_i[0][lane / MD_SITE_VEC][lane % MD_SITE_VEC] = sd[(uint32_t)i * sstride + lane];
         site_i[1][lane / MD_SITE_VEC][lane % MD_SITE_VEC] = se[(uint32_t)i * sstride + lane];
     }
@@ -1836,8 +1836,8 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
             const SigDyn B{cP.comp[cj], cj};
             ms_molpair<Real>(A, B, da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, u6p, uxp, rfp, n);
         };
-        ms_molecule<Real>(S, xlf, sd, se, sstride, nbr, nnb, maxnb, soff, ring[wl], site_i[wl], lane, i, A, epsRF, W,
-                          pair);
+        ms_molecule<Real>(S, xlf, sd, se, sstride, nbr, nnb, maxnb, soff, ring[wl], site_i[wl], lane, i, A.ns(), epsRF,
+                          W, pair);
     }
     ms_store_partials<Real>(partials, pstride, W);
 }
@@ -1853,19 +1853,19 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
     for (int t = 0; t < MS_MOLS; ++t) {
         const int64_t i = w * MS_MOLS + t;
         if (i >= S.n) break;  // warp-uniform
-        auto run = [&](auto A) {
-            auto pair = [&](int cj, const Real (*da_t)[3], const Real (*ea_t)[3], uint32_t jb, const Real* md, int fl,
-                            bool macro, Real eps, Real* fp, Real* mp, Real& u6p, Real& uxp, Real& rfp, MsCounts& n) {
-                if (cj == 0)
-                    ms_molpair<Real>(A, S0(), da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, u6p, uxp, rfp, n);
-                else
-                    ms_molpair<Real>(A, S1(), da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, u6p, uxp, rfp, n);
-            };
-            ms_molecule<Real>(S, xlf, sd, se, sstride, nbr, nnb, maxnb, soff, ring[wl], site_i[wl], lane, i, A, epsRF,
-                              W, pair);
+        const int ci = S.comp[i];
+        // one instance of the site-pair code per (home, neighbour) signature pair; the molecule-level code around
+        // it exists once
+        auto pair = [&](int cj, const Real (*da_t)[3], const Real (*ea_t)[3], uint32_t jb, const Real* md, int fl,
+                        bool macro, Real eps, Real* fp, Real* mp, Real& u6p, Real& uxp, Real& rfp, MsCounts& n) {
+            DispFix2<S0, S1>::run(ci, [&](auto A) {
+                DispFix2<S0, S1>::run(cj, [&](auto B) {
+                    ms_molpair<Real>(A, B, da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, u6p, uxp, rfp, n);
+                });
+            });
         };
-        if (S.comp[i] == 0) run(S0());
-        else run(S1());
+        ms_molecule<Real>(S, xlf, sd, se, sstride, nbr, nnb, maxnb, soff, ring[wl], site_i[wl], lane, i,
+                          cP.comp[ci].ns, epsRF, W, pair);
     }
     ms_store_partials<Real>(partials, pstride, W);
 }
