@@ -1580,10 +1580,16 @@ struct SigFix {
 };
 
 // Signature dispatch by component index: DispDyn hands `f` the run-time
-// signature; DispFix2<S0, S1> the compile-time one of a two-component system.
+// signature; DispFix2<S0, S1> the compile-time one of a two-component system;
+// DispOne<S0> always S0 (kernels launched for one component's molecules).
 struct DispDyn {
     template <class F>
     __device__ __forceinline__ static void run(int c, F f) { f(SigDyn{cP.comp[c], c}); }
+};
+template <class S0>
+struct DispOne {
+    template <class F>
+    __device__ __forceinline__ static void run(int, F f) { f(S0()); }
 };
 template <class S0, class S1>
 struct DispFix2 {
