@@ -1454,21 +1454,10 @@ __device__ __forceinline__ int ms_flags(const State& S, int64_t i, uint32_t e, c
 // 64 (entry + flags) in row order; every full group of 32 is handed to
 // `body(entry, flags, m_d)`, one candidate per lane, and the rest (< 32) at
 // the end to the lanes below the count.
-// The L1 prefetch of an accepted neighbour's component and site records
-// (its slot's records of the two site arrays), issued when the row walk
-// accepts it and ahead of the body that reads them.
-template <typename Real>
-__device__ __forceinline__ void ms_prefetch(const int* comp, const Real* sd, const Real* se, uint32_t sstride,
-                                            uint32_t j) {
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(comp + j));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(sd + j * sstride));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(se + j * sstride));
-}
-
-template <typename Real, typename Body, typename Pre>
+template <typename Real, typename Body>
 __device__ __forceinline__ void ms_walk_row(const State& S, const float4* xlf, const Real (*soff)[3], const Real* pi,
                                             int64_t i, const uint32_t* row, int cnt, uint32_t* ring, int lane,
-                                            Body body, Pre pre) {
+                                            Body body) {
     int head = 0, qn = 0;
     const unsigned lt = (1u << lane) - 1u;
     for (int k0 = 0; k0 < cnt; k0 += 32) {
@@ -1486,7 +1475,6 @@ __device__ __forceinline__ void ms_walk_row(const State& S, const float4* xlf, c
             const int p = (head + qn + __popc(bal & lt)) & 63;
             ring[p] = e;
             ring[64 + p] = (uint32_t)fl;
-            pre(e & MD_INDEX_MASK);
         }
         qn += __popc(bal);
         __syncwarp();
@@ -1792,8 +1780,7 @@ __device__ __forceinline__ void ms_molecule(const State& S, const float4* xlf, c
             W.vir.add(vp[0] + vp[1] + vp[2]);
         }
     };
-    ms_walk_row<Real>(S, xlf, soff, pi, i, nbr + (size_t)i * maxnb, nnb[i], ring, lane, body,
-                      [&](uint32_t j) { ms_prefetch<Real>(S.comp, sd, se, sstride, j); });
+    ms_walk_row<Real>(S, xlf, soff, pi, i, nbr + (size_t)i * maxnb, nnb[i], ring, lane, body);
     const double fx = warp_total_plain(F[0]), fy = warp_total_plain(F[1]), fz = warp_total_plain(F[2]);
     const double mx = warp_total_plain(M[0]), my = warp_total_plain(M[1]), mz = warp_total_plain(M[2]);
     const double vx = warp_total_plain(V[0], 0.5f), vy = warp_total_plain(V[1], 0.5f), vz = warp_total_plain(V[2], 0.5f);
