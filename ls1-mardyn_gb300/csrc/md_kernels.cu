@@ -845,10 +845,6 @@ __device__ __forceinline__ double fp64_r2(const State& S, int64_t i, int64_t j, 
     return __dadd_rn(__dmul_rn(dx, dx), __dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dz, dz)));
 }
 
-template <typename Real> struct R4;
-template <> struct R4<float> { typedef float4 t; };
-template <> struct R4<double> { typedef double4 t; };
-
 // Single-LJ-centre molecules (centre at the molecule origin), FP32 pair
 // arithmetic: the hot kernel of the 1CLJ benchmarks.  One thread per
 // molecule streams its candidate row four entries per 16-byte load, gathers
