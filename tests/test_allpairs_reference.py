@@ -26,6 +26,9 @@ def systems(name):
         ps = psm.lj_fcc(5, 0.7, 1.1, seed=3)
         ps.r = ps.r + np.random.default_rng(3).uniform(-0.15, 0.15, ps.r.shape)
         return ps, 2.5
+    if name == "offcentre":
+        from systems import offcentre_mixture
+        return offcentre_mixture(), 1.0
     return psm.mixture(2000, 14.0, 300.0, seed=4), 1.0
 
 
@@ -56,7 +59,7 @@ def oracle_state(ps, rc):
     return fo.upot, fo.virial, m["F"][order], m["M"][order]
 
 
-@pytest.mark.parametrize("name", ["lj", "mixture"])
+@pytest.mark.parametrize("name", ["lj", "mixture", "offcentre"])
 def test_allpairs_matches_the_oracle(name):
     ps, rc = systems(name)
     F, M, U, W = AllPairs(ps, rc).forces_torques()
@@ -64,11 +67,11 @@ def test_allpairs_matches_the_oracle(name):
     assert abs(U - Uo) <= 1e-12 * abs(Uo)
     assert abs(W - Wo) <= 1e-12 * abs(Wo)
     assert np.abs(F - Fo).max() <= 1e-12 * np.abs(Fo).max()
-    if name == "mixture":
+    if name != "lj":
         assert np.abs(M - Mo).max() <= 1e-12 * np.abs(Mo).max()
 
 
-@pytest.mark.parametrize("name", ["lj", "mixture"])
+@pytest.mark.parametrize("name", ["lj", "mixture", "offcentre"])
 def test_allpairs_parameter_gradients_vs_oracle_finite_differences(name):
     """Central differences with h = 1e-5 |p| (truncation and rounding both
     near 1e-9 relative here)."""

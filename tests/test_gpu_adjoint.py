@@ -150,10 +150,13 @@ def _oracle_uw(ps, rc):
 def _system(name):
     if name == "lj":
         return lj_box(), 2.5
+    if name == "offcentre":
+        from systems import offcentre_mixture
+        return offcentre_mixture(), 1.0
     return psm.mixture(2000, 14.0, 300.0, seed=4), 1.0
 
 
-@pytest.mark.parametrize("name", ["lj", "mixture"])
+@pytest.mark.parametrize("name", ["lj", "mixture", "offcentre"])
 def test_parameter_gradients_vs_oracle_finite_differences(E, name):
     """dUpot/dp and dvirial/dp for every site parameter (eps and sigma of each
     LJ centre, |Q| of the quadrupole, |mu| of the dipole) against central
@@ -176,16 +179,21 @@ def test_parameter_gradients_vs_oracle_finite_differences(E, name):
         assert abs(gpW[k] - fw) <= 5e-8 * abs(fw), (k, gpW[k], fw)
 
 
+@pytest.mark.parametrize("system", ["mixture", "offcentre"])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 2e-4)])
-def test_mixture_against_fp64_all_pairs_torch_reference(E, precision, tol):
-    """2,048-molecule 2CLJQ + 1CLJD mixture: position gradients (with a force
-    cotangent gF, i.e. the pair Hessian-vector products of the LJ, dipole and
-    quadrupole bodies) and parameter gradients of the adjoint against the FP64
-    all-pairs torch reference, for three (gU, gW, gF) combinations.  FP64:
-    per parameter 1e-9 relative; mixed: 2e-4 of the largest."""
+def test_mixture_against_fp64_all_pairs_torch_reference(E, precision, tol, system):
+    """2,048-molecule 2CLJQ + 1CLJD mixture (multipoles at the molecule
+    centres: without gF its multipole Hessian-vector products take the
+    homogeneity shortcut) and a 1,372-molecule mixture with off-centre
+    dipoles and quadrupoles (tests/systems.py; dual numbers throughout):
+    position gradients (with a force cotangent gF, i.e. the pair
+    Hessian-vector products of the LJ, dipole and quadrupole bodies) and
+    parameter gradients of the adjoint against the FP64 all-pairs torch
+    reference, for three (gU, gW, gF) combinations.  FP64: per parameter
+    1e-9 relative; mixed: 2e-4 of the largest."""
     pytest.importorskip("torch")
     from oracle.allpairs import AllPairs
-    ps, rc = _system("mixture")
+    ps, rc = _system(system)
     ap = AllPairs(ps, rc)
     gF = np.random.default_rng(17).normal(size=(ps.n, 3))
     e, U, W = forward(E, ps, rc, precision)
