@@ -606,9 +606,7 @@ __device__ __forceinline__ void test_staged(int m, const float2 pix, const float
                                             bool own, uint32_t self, uint32_t* buf, int& nb, int& cnt, uint32_t* row,
                                             int maxnb) {
     uint32_t hits = 0u;
-    const int mm = (m + 1) & ~1;  // pairs of staged slots; slot m (if odd) is far away
-#pragma unroll 4
-    for (int t = 0; t < mm; t += 2) {
+    auto test2 = [&](int t) {
         const float2 dx = __fadd2_rn(pix, *reinterpret_cast<const float2*>(sx + t));
         const float2 dy = __fadd2_rn(piy, *reinterpret_cast<const float2*>(sy + t));
         const float2 dz = __fadd2_rn(piz, *reinterpret_cast<const float2*>(sz + t));
@@ -617,6 +615,14 @@ __device__ __forceinline__ void test_staged(int m, const float2 pix, const float
         r2 = __ffma2_rn(dx, dx, r2);
         hits |= (r2.x < rl2 ? 1u : 0u) << t;
         hits |= (r2.y < rl2 ? 1u : 0u) << (t + 1);
+    };
+    if (m == 32) {  // a full staging area (the common case): bit positions known at compile time
+#pragma unroll
+        for (int t = 0; t < 32; t += 2) test2(t);
+    } else {
+        const int mm = (m + 1) & ~1;  // pairs of staged slots; slot m (if odd) is far away
+#pragma unroll 4
+        for (int t = 0; t < mm; t += 2) test2(t);
     }
     if (!own) hits = 0u;
     while (hits) {
