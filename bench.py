@@ -24,6 +24,9 @@ forces, post-force half step and the Upot/virial/kinetic sums.
           force error, Upot / virial / pressure errors, pair counts;
   fp64   the same workload through the FP64 kernel (molecule-updates/s), and
           the adjoint / forward pair-kernel time ratio;
+  mixture, batch  the 1M 2CLJQ/1CLJD mixture (device-timed steps, the
+          multi-site pair kernel's FP32 roofline fraction, its errors against
+          FP64) and the 512-box batch (autotuned, device-timed), in short;
   cpu_baseline  the CPU oracle (C restatement of the reference's path, OpenMP
           C08 traversal) on all host cores on the full workload for as many
           steps as fit in a bounded time.
@@ -451,6 +454,65 @@ def graph_node_us(device: int, nodes: int = 400) -> float:
     return best * 1e3 / nodes
 
 
+def mixture_summary(local: int, steps: int = 20) -> dict:
+    """The 1M 2CLJQ/1CLJD mixture (the mix1m workload) in short: device-timed
+    NVE steps after a warm-up, the multi-site pair kernel's time and FP32
+    roofline fraction, and its mixed-precision errors against FP64."""
+    from ls1gb300 import engine as E
+    from ls1gb300 import precision as P
+    cu = Cudart()
+    gen, rc, dt, desc = WORKLOADS["mix1m"]
+    ps = gen()
+    skin = DEFAULT_SKIN["mix1m"]
+    e = E.Engine(ps, rc, precision="mixed", skin=skin, device=local)
+    e.forces()
+    e.run(dt, 5, record=False)
+    st = e.stream()
+    c0, c1 = cu.event(), cu.event()
+    cu.record(c0, st)
+    e.run(dt, steps, record=True)
+    cu.record(c1, st)
+    ms = cu.elapsed_ms(c0, c1)
+    fo = e.forces()
+    kt = e.time_kernels(5)
+    mol = e.molecules()
+    e.close()
+    flops = FLOP_PER_MOL_PAIR * fo.mol_pairs + sum(f * k for f, k in zip(FLOP_PER_SITE_PAIR, fo.site_pairs))
+    sms, mhz = cu.attr(16, local), cu.attr(13, local) / 1e3
+    peak = sms * FP32_LANES_PER_SM * 2 * mhz * 1e6 / 1e12
+    tflops = flops / (kt.force_ms * 1e-3) / 1e12
+    prec = P.report(P.state_of(mol, ps), rc, skin=skin, device=local, mixed_forces=(fo, mol))
+    return {"workload": desc, "molecules": ps.n, "value": ps.n * steps / (ms * 1e-3),
+            "unit": "molecule-updates/s", "ms_per_step": ms / steps, "steps": steps,
+            "pair_kernel_ms": kt.force_ms, "pair_kernel_tflops": tflops,
+            "pair_kernel_frac_fp32": tflops / peak, "fp32_peak_note": "nominal FP32 FMA rate at the device's maximum clock",
+            "precision": prec}
+
+
+def batch_summary(local: int, steps: int = 100) -> dict:
+    """The 512-box batch (the batch512 workload) in short: autotuned, then
+    device-timed steps in graphs of 100."""
+    from ls1gb300 import batch as B
+    cu = Cudart()
+    boxes = B.random_boxes(512, 500, 20000, seed=2024)
+    n = sum(b.n for b in boxes)
+    dt = 0.002
+    bt = B.Batch(boxes, 2.5, precision="mixed", device=local)
+    bt.forces()
+    tune = bt.autotune(dt, trial_steps=30)
+    bt.forces()
+    bt.run(dt, 10, graph_steps=100, record=False)
+    st = bt.stream()
+    c0, c1 = cu.event(), cu.event()
+    cu.record(c0, st)
+    bt.run(dt, steps, graph_steps=100, record=True)
+    cu.record(c1, st)
+    ms = cu.elapsed_ms(c0, c1)
+    bt.close()
+    return {"workload": BATCH_DESC, "boxes": len(boxes), "molecules": n, "value": n * steps / (ms * 1e-3),
+            "unit": "molecule-updates/s", "ms_per_step": ms / steps, "steps": steps, "autotune": tune}
+
+
 def _perturbed(ps, f: float):
     """The phase space with every LJ eps, sigma and multipole magnitude scaled by f."""
     import copy
@@ -717,6 +779,12 @@ def main():
                    "kernel_forward_ms": ktm.force_ms, "kernel_adjoint_ms": ktm.adjoint_ms,
                    "adjoint_over_forward": ktm.adjoint_ms / ktm.force_ms}
 
+    # the multi-site mixture and the box batch in short, so that one default run records every workload's figure
+    mixture, batch = None, None
+    if a.workload == "lj4m" and a.precision == "mixed" and not rmm and world == 1:
+        mixture = mixture_summary(local)
+        batch = batch_summary(local)
+
     # ---- end to end through the C ABI with host buffers
     e2e = None
     if not a.no_e2e:
@@ -787,6 +855,8 @@ def main():
             "precision": prec,
             "fp64": fp64,
             "newton3": newton3,
+            "mixture": mixture,
+            "batch": batch,
             "adjoint": {"lj": adj, "mixture": adj_mix,
                         "value": max(x["adjoint_over_forward"] for x in (adj, adj_mix) if x),
                         "unit": "adjoint / forward pair-kernel time"},
