@@ -84,10 +84,14 @@ typedef struct {
     int32_t pair_scheme;/* MD_PAIRS_ROWS (0): per-molecule candidate rows, each pair
                            evaluated from both sides; MD_PAIRS_NEWTON3 (1): every pair
                            evaluated once (Newton's third law, as
-                           VectorizedCellProcessor::processCellPair, VCP.cpp:2744-2819) by
-                           cluster pairs where the system allows (one component of
-                           single-centre LJ molecules, mixed precision, rc_lj = rc, at least
-                           three list cells per periodic dimension), rows elsewhere         */
+                           VectorizedCellProcessor::processCellPair, VCP.cpp:2744-2819),
+                           mixed precision only, with at least three list cells per periodic
+                           dimension: by cluster pairs for one component of single-centre
+                           LJ molecules with rc_lj = rc; by the higher-slot half of each
+                           row, the neighbour's force, torque and virial added by FP32
+                           atomics, for multi-site molecules; rows elsewhere.  The
+                           atomics' order varies, so results agree between runs to FP32
+                           rounding rather than bit for bit                                 */
 } md_config;
 
 #define MD_PAIRS_ROWS 0
@@ -402,7 +406,8 @@ typedef struct {
                                  half-step kernel (cluster pairs); 0 otherwise          */
     double lf_ms;             /* cluster pairs: that half-step kernel alone; 0 otherwise */
     int32_t pair_scheme;      /* the scheme the context's pair evaluations use now:
-                                 MD_PAIRS_NEWTON3 (cluster pairs) or MD_PAIRS_ROWS       */
+                                 MD_PAIRS_NEWTON3 (cluster pairs, or half rows of
+                                 multi-site molecules) or MD_PAIRS_ROWS                  */
     int32_t cluster_size;     /* molecules per cluster of the Newton-3 path             */
 } md_kernel_times;
 

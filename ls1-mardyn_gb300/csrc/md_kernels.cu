@@ -1367,8 +1367,13 @@ __global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __res
 // Stable partition of every candidate row by the neighbour's component (one
 // warp per molecule; the row is staged in dynamic shared memory, maxnb
 // entries per warp).  Only the order within a row changes.
+#define ROW_PART_SMEM (48 * 1024)  // shared bytes per block of k_row_partition (rows staged whole)
+
+// With nhalf (the multi-site kernels' Newton-3 form) each row is first split
+// into the neighbours in higher slots and those in lower slots, each part
+// partitioned by component; nhalf[i] = the length of the first part.
 __global__ void k_row_partition(int64_t n, const float4* __restrict__ xl, uint32_t* nbr, const int* nnb, int maxnb,
-                                int ncomp, const unsigned* need) {
+                                int ncomp, const unsigned* need, int* nhalf) {
     if (!*need) return;
     extern __shared__ uint32_t rowbuf[];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1380,19 +1385,24 @@ __global__ void k_row_partition(int64_t n, const float4* __restrict__ xl, uint32
     for (int k = lane; k < cnt; k += 32) buf[k] = row[k];
     __syncwarp();
     int out = 0;
-    for (int c = 0; c < ncomp; ++c) {
-        for (int k0 = 0; k0 < cnt; k0 += 32) {
-            const int k = k0 + lane;
-            uint32_t e = 0u;
-            bool m = false;
-            if (k < cnt) {
-                e = buf[k];
-                m = __float_as_int(__ldg(&xl[e & MD_INDEX_MASK]).w) == c;
+    const int parts = nhalf ? 2 : 1;
+    for (int h = 0; h < parts; ++h) {
+        for (int c = 0; c < ncomp; ++c) {
+            for (int k0 = 0; k0 < cnt; k0 += 32) {
+                const int k = k0 + lane;
+                uint32_t e = 0u;
+                bool m = false;
+                if (k < cnt) {
+                    e = buf[k];
+                    const int64_t j = e & MD_INDEX_MASK;
+                    m = (ncomp == 1 || __float_as_int(__ldg(&xl[j]).w) == c) && (!nhalf || (j > i) == (h == 0));
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, m);
+                if (m) row[out + __popc(bal & ((1u << lane) - 1u))] = e;
+                out += __popc(bal);
             }
-            const unsigned bal = __ballot_sync(0xffffffffu, m);
-            if (m) row[out + __popc(bal & ((1u << lane) - 1u))] = e;
-            out += __popc(bal);
         }
+        if (nhalf && h == 0 && lane == 0) nhalf[i] = out;
     }
 }
 
@@ -1545,6 +1555,9 @@ static_assert(MD_SITE_VEC * MD_MAXS <= 32, "one lane per element loads the warp 
 #define MS_ADJ_MIN_BLOCKS 5  // FP32 adjoint kernel: the same (96 registers, no spills)
 #endif
 #define MS_ADJ_MIN_MOLS 8  // fewest molecules per warp of the multi-site adjoint
+#ifndef MS_N3_MIN_BLOCKS
+#define MS_N3_MIN_BLOCKS 5  // FP32 Newton-3 force kernel: the same (96 registers, no spills)
+#endif
 
 // Site signature of a component as the multi-site kernels read it (sites in
 // the order LJ centres, charges, dipoles, quadrupoles): SigDyn reads the
@@ -1613,12 +1626,23 @@ struct MsCounts {
 // site before its lever-arm torque; the virial of the molecule pair is
 // m_d o (sum of its site forces).  fp, mp: force and torque on the home
 // molecule; u6p, uxp, rfp: its LJ (times 6), multipole and reaction-field
-// energies.
-template <typename Real, class SA, class SB>
+// energies.  With N3 also mq, the torque on the neighbour about its centre
+// (the reference's Newton-3 half of processCellPair, VCP.cpp:2744-2819):
+// per site pair f_a x d_b (the force -f_a acts at the neighbour's site
+// offset d_b) plus the body's multipole torque on site b.
+template <typename Real, bool N3 = false, class SA, class SB>
 __device__ __forceinline__ void ms_molpair(const SA& A, const SB& B, const Real (*da_t)[3], const Real (*ea_t)[3],
                                            const Real* sd, const Real* se, uint32_t jb, const Real* md, int fl,
-                                           bool macro, Real epsRF, Real* fp, Real* mp, Real& u6p, Real& uxp, Real& rfp,
-                                           MsCounts& n) {
+                                           bool macro, Real epsRF, Real* fp, Real* mp, Real* mq, Real& u6p, Real& uxp,
+                                           Real& rfp, MsCounts& n) {
+    // torque on the neighbour of the force fs on the home site (sign sg) at its site offset db, plus tb
+    auto jtorque = [&](const Real* fs, Real sg, const Real* db, const Real* tb) {
+        if (!N3) return;
+        mq[0] += sg * (fs[1] * db[2] - fs[2] * db[1]);
+        mq[1] += sg * (fs[2] * db[0] - fs[0] * db[2]);
+        mq[2] += sg * (fs[0] * db[1] - fs[1] * db[0]);
+        if (tb) { mq[0] += tb[0]; mq[1] += tb[1]; mq[2] += tb[2]; }
+    };
     if (fl & 1) {
         const int nlb = B.nlj();
         for (int a = 0; a < A.nlj(); ++a) {
@@ -1635,6 +1659,7 @@ __device__ __forceinline__ void ms_molpair(const SA& A, const SB& B, const Real 
                               PTab<Real>::shift6(cP, row + b), f, Vd, u);
                 fa[0] += f[0]; fa[1] += f[1]; fa[2] += f[2];
                 u6p += u;
+                jtorque(f, (Real)1, db, nullptr);
             }
             mp[0] += da[1] * fa[2] - da[2] * fa[1];
             mp[1] += da[2] * fa[0] - da[0] * fa[2];
@@ -1651,9 +1676,9 @@ __device__ __forceinline__ void ms_molpair(const SA& A, const SB& B, const Real 
             const Real* ea = ea_t[a];
             const Real pa = PTab<Real>::p(cP, A.comp(), a);
             Real fa[3] = {0, 0, 0}, ta[3] = {0, 0, 0};
+            Real db[3];
             auto site_j = [&](int b, Real* ds, Real* eb) {
                 const uint32_t ob = jb + MD_SITE_VEC * (uint32_t)b;
-                Real db[3];
                 site_rec<Real>(sd + ob, db);
                 site_rec<Real>(se + ob, eb);
                 for (int c = 0; c < 3; ++c) ds[c] = md[c] + (da[c] - db[c]);
@@ -1665,18 +1690,21 @@ __device__ __forceinline__ void ms_molpair(const SA& A, const SB& B, const Real 
                     cc_body<Real>(ds, pa, PTab<Real>::p(cP, B.comp(), b), f, u);
                     for (int c = 0; c < 3; ++c) fa[c] += f[c];
                     uxp += u;
+                    jtorque(f, (Real)1, db, nullptr);
                 }
                 for (int b = b1; b < b2; ++b) {
                     site_j(b, ds, eb);
                     cd_body<Real>(ds, pa, eb, PTab<Real>::p(cP, B.comp(), b), f, Tj, u);
                     for (int c = 0; c < 3; ++c) fa[c] += f[c];
                     uxp += u;
+                    jtorque(f, (Real)1, db, Tj);
                 }
                 for (int b = b2; b < b3; ++b) {
                     site_j(b, ds, eb);
                     cq_body<Real>(ds, pa, eb, PTab<Real>::p(cP, B.comp(), b), f, Tj, u);
                     for (int c = 0; c < 3; ++c) fa[c] += f[c];
                     uxp += u;
+                    jtorque(f, (Real)1, db, Tj);
                 }
                 if (macro) { n.cc += B.nch(); n.cd += B.ndi(); n.cq += B.nqu(); }
             } else if (ka == SK_DIPOLE) {
@@ -1686,19 +1714,22 @@ __device__ __forceinline__ void ms_molpair(const SA& A, const SB& B, const Real 
                     cd_body<Real>(nd, PTab<Real>::p(cP, B.comp(), b), ea, pa, f, T, u);
                     for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
                     uxp += u;
+                    jtorque(f, (Real)-1, db, nullptr);
                 }
                 for (int b = b1; b < b2; ++b) {
                     site_j(b, ds, eb);
-                    dd_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, B.comp(), b), epsRF, f, T, u, urf);
+                    dd_body<Real, N3>(ds, ea, pa, eb, PTab<Real>::p(cP, B.comp(), b), epsRF, f, T, u, urf, Tj);
                     for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
                     uxp += u;
                     rfp += urf;
+                    jtorque(f, (Real)1, db, Tj);
                 }
                 for (int b = b2; b < b3; ++b) {
                     site_j(b, ds, eb);
                     dq_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, B.comp(), b), f, T, Tj, u);
                     for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
                     uxp += u;
+                    jtorque(f, (Real)1, db, Tj);
                 }
                 if (macro) { n.cd += B.nch(); n.dd += B.ndi(); n.dq += B.nqu(); }
             } else {
@@ -1708,6 +1739,7 @@ __device__ __forceinline__ void ms_molpair(const SA& A, const SB& B, const Real 
                     cq_body<Real>(nd, PTab<Real>::p(cP, B.comp(), b), ea, pa, f, T, u);
                     for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
                     uxp += u;
+                    jtorque(f, (Real)-1, db, nullptr);
                 }
                 for (int b = b1; b < b2; ++b) {
                     site_j(b, ds, eb);
@@ -1715,12 +1747,14 @@ __device__ __forceinline__ void ms_molpair(const SA& A, const SB& B, const Real 
                     dq_body<Real>(nd, eb, PTab<Real>::p(cP, B.comp(), b), ea, pa, f, Tj, T, u);
                     for (int c = 0; c < 3; ++c) { fa[c] -= f[c]; ta[c] += T[c]; }
                     uxp += u;
+                    jtorque(f, (Real)-1, db, Tj);
                 }
                 for (int b = b2; b < b3; ++b) {
                     site_j(b, ds, eb);
                     qq_body<Real>(ds, ea, pa, eb, PTab<Real>::p(cP, B.comp(), b), f, T, Tj, u);
                     for (int c = 0; c < 3; ++c) { fa[c] += f[c]; ta[c] += T[c]; }
                     uxp += u;
+                    jtorque(f, (Real)1, db, Tj);
                 }
                 if (macro) { n.cq += B.nch(); n.dq += B.ndi(); n.qq += B.nqu(); }
             }
@@ -1732,6 +1766,16 @@ __device__ __forceinline__ void ms_molpair(const SA& A, const SB& B, const Real 
         }
     }
 }
+
+// Outputs of the multi-site kernels' Newton-3 form (md_config.pair_scheme =
+// MD_PAIRS_NEWTON3): nh = the length of each row's leading part that holds
+// the neighbours in higher slots (k_row_partition), and FP32 accumulators of
+// the force, torque and virial that the neighbours of lower slots add to a
+// molecule (cleared by k_ms_n3_store, which adds them to the state).
+struct MsN3Out {
+    const int* nh;
+    float4 *f, *m, *v;
+};
 
 // Per-warp state of the multi-site force kernels.
 template <typename Real>
@@ -1769,9 +1813,9 @@ __device__ __forceinline__ void ms_molecule(const State& S, const float4* xlf, c
     auto body = [&](uint32_t e, int fl, const Real* md) {
         const uint32_t j = e & MD_INDEX_MASK;
         const bool macro = (int64_t)j > i;
-        Real fp[3] = {0, 0, 0}, mp[3] = {0, 0, 0};
+        Real fp[3] = {0, 0, 0}, mp[3] = {0, 0, 0}, mq[3] = {0, 0, 0};
         Real u6p = 0, uxp = 0, rfp = 0;
-        pair(S.comp[j], site_i[0], site_i[1], j * sstride, md, fl, macro, epsRF, fp, mp, u6p, uxp, rfp, W.n);
+        pair(S.comp[j], site_i[0], site_i[1], j * sstride, md, fl, macro, epsRF, fp, mp, mq, u6p, uxp, rfp, W.n);
         const Real vp[3] = {md[0] * fp[0], md[1] * fp[1], md[2] * fp[2]};
         for (int c = 0; c < 3; ++c) { F[c] += fp[c]; M[c] += mp[c]; V[c] += vp[c]; }
         if (macro) {
@@ -1824,28 +1868,169 @@ __device__ __forceinline__ void ms_store_partials(double* partials, int pstride,
     /* site records [slot][site][MD_SITE_VEC]; the host keeps cap * stride * MD_SITE_VEC < 2^32 */ \
     const uint32_t sstride = MD_SITE_VEC * (uint32_t)stride;
 
+// The Newton-3 form of a warp's molecules base .. base + nmol - 1 (FP32).
+// Each half row holds about half the in-cut-off neighbours of a full row, so
+// one molecule's neighbours would leave most of its last group of 32 lanes
+// idle; the ring of in-cut-off candidates therefore runs on across the warp's
+// molecules, each entry tagged with its home molecule t (site records of all
+// of them staged in shared memory, sites[t]), and every group of 32 lanes
+// evaluates 32 molecule pairs of one or several homes.  The home's share of a
+// group (F, M, m_d o F) is summed per home by a segmented warp scan (the tags
+// of a group are contiguous and ascending) and added by the segment's last
+// lane to the home's shared accumulator acc[t]; the neighbour's share goes to
+// its global accumulators in o.  `pair(ci, cj, ...)` evaluates one molecule
+// pair as in ms_molecule.
+template <class Pair>
+__device__ __forceinline__ void ms_warp_n3(const State& S, const float4* xlf, const float* sd, const float* se,
+                                           uint32_t sstride, const uint32_t* nbr, int maxnb,
+                                           const float (*soff)[3], uint32_t* ring, float (*sites)[2][MD_MAXS][3],
+                                           float (*acc)[9], int lane, int64_t base, int nmol, float epsRF,
+                                           MsWarp<float>& W, MsN3Out o, Pair pair) {
+    const unsigned FULL = 0xffffffffu;
+    // site records and accumulators of the warp's molecules
+    __syncwarp();
+    for (uint32_t k = lane; k < (uint32_t)nmol * sstride; k += 32) {
+        const uint32_t t = k / sstride, r = k % sstride, a = r / MD_SITE_VEC, c = r % MD_SITE_VEC;
+        if (c < 3 && a < MD_MAXS) {
+            sites[t][0][a][c] = sd[(uint32_t)base * sstride + k];
+            sites[t][1][a][c] = se[(uint32_t)base * sstride + k];
+        }
+    }
+    for (int k = lane; k < 32 * 9; k += 32) acc[k / 9][k % 9] = 0.f;
+    __syncwarp();
+    int head = 0, qn = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    // one group: the ring's next nl entries, one per lane
+    auto group = [&](int nl) {
+        const int p = (head + lane) & 63;
+        const uint32_t e = ring[p], tf = ring[64 + p];
+        __syncwarp();
+        head = (head + nl) & 63;
+        qn -= nl;
+        const bool act = lane < nl;
+        const int t = act ? (int)(tf >> 2) : 32 + lane;  // idle lanes: tags of their own above every home's
+        float v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (act) {
+            const int64_t i = base + t;
+            const uint32_t j = e & MD_INDEX_MASK;
+            const float4 p4 = xlf[i];
+            const float pi[3] = {p4.x, p4.y, p4.z};
+            float md[3];
+            ms_centre_distance<float>(S, xlf, soff, pi, i, e, md);
+            float fp[3] = {0, 0, 0}, mp[3] = {0, 0, 0}, mq[3] = {0, 0, 0};
+            float u6p = 0, uxp = 0, rfp = 0;
+            const bool macro = (int64_t)j > i;  // always: the half rows hold higher slots only
+            pair(S.comp[i], S.comp[j], sites[t][0], sites[t][1], j * sstride, md, (int)(tf & 3u), macro, epsRF, fp,
+                 mp, mq, u6p, uxp, rfp, W.n);
+            const float vp[3] = {md[0] * fp[0], md[1] * fp[1], md[2] * fp[2]};
+            if (macro) {
+                if (tf & 2u) W.n.mol += 1;
+                W.u6.add(u6p);
+                W.ux.add(uxp);
+                W.rf.add(rfp);
+                W.vir.add(vp[0] + vp[1] + vp[2]);
+            }
+            atomicAdd(&o.f[j], make_float4(-fp[0], -fp[1], -fp[2], 0.f));
+            atomicAdd(&o.m[j], make_float4(mq[0], mq[1], mq[2], 0.f));
+            atomicAdd(&o.v[j], make_float4(0.5f * vp[0], 0.5f * vp[1], 0.5f * vp[2], 0.f));
+            for (int c = 0; c < 3; ++c) { v[c] = fp[c]; v[3 + c] = mp[c]; v[6 + c] = vp[c]; }
+        }
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int tu = __shfl_up_sync(FULL, t, off);
+            const bool same = lane >= off && tu == t;
+#pragma unroll
+            for (int c = 0; c < 9; ++c) {
+                const float u = __shfl_up_sync(FULL, v[c], off);
+                if (same) v[c] += u;
+            }
+        }
+        const int tn = __shfl_down_sync(FULL, t, 1);
+        if (act && (lane == 31 || tn != t)) {  // last lane of its home's segment (distinct homes)
+#pragma unroll
+            for (int c = 0; c < 9; ++c) acc[t][c] += v[c];
+        }
+        __syncwarp();
+    };
+    for (int t = 0; t < nmol; ++t) {
+        const int64_t i = base + t;
+        const float4 p4 = xlf[i];
+        const float pi[3] = {p4.x, p4.y, p4.z};
+        const uint32_t* row = nbr + (size_t)i * maxnb;
+        const int cnt = o.nh[i];
+        for (int k0 = 0; k0 < cnt; k0 += 32) {
+            const int k = k0 + lane;
+            int fl = 0;
+            uint32_t e = 0u;
+            if (k < cnt) {
+                e = __ldg(&row[k]);
+                float md[3];
+                ms_centre_distance<float>(S, xlf, soff, pi, i, e, md);
+                fl = ms_flags<float>(S, i, e, md);
+            }
+            const unsigned bal = __ballot_sync(FULL, fl != 0);
+            if (fl) {
+                const int q = (head + qn + __popc(bal & lt)) & 63;
+                ring[q] = e;
+                ring[64 + q] = (uint32_t)fl | ((uint32_t)t << 2);
+            }
+            qn += __popc(bal);
+            __syncwarp();
+            if (qn >= 32) group(32);
+        }
+    }
+    if (qn > 0) group(qn);
+    // the homes' sums into the state (the neighbours' shares follow in k_ms_n3_store)
+    if (lane < nmol) {
+        const int64_t i = base + lane;
+        const float* a = acc[lane];
+        S.Fx[i] = f2d_exact(a[0]); S.Fy[i] = f2d_exact(a[1]); S.Fz[i] = f2d_exact(a[2]);
+        S.Mx[i] = f2d_exact(a[3]); S.My[i] = f2d_exact(a[4]); S.Mz[i] = f2d_exact(a[5]);
+        S.Vx[i] = f2d_exact(0.5f * a[6]); S.Vy[i] = f2d_exact(0.5f * a[7]); S.Vz[i] = f2d_exact(0.5f * a[8]);
+    }
+    __syncwarp();
+}
+
 // General multi-site molecules: all site pairs of every molecule pair inside
 // the molecule-centre cut-off (rc_lj for LJ centres, rc for the multipoles),
 // with calcFM folded in: F = sum f, M = sum d_site x f + multipole torques,
 // Vi = 1/2 sum m_d o f.  One warp per molecule, 32 molecules per warp one
 // after another; component signatures read at run time.
-template <typename Real>
-__global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOCKS : 3) k_force_ms(State S, const float4* xlf, const Real* sd, const Real* se,
+template <typename Real, bool N3 = false>
+__global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? (N3 ? MS_N3_MIN_BLOCKS : MS_MIN_BLOCKS) : 3) k_force_ms(State S, const float4* xlf, const Real* sd, const Real* se,
                                                             int stride, const uint32_t* nbr, const int* nnb, int maxnb,
-                                                            double* partials, int pstride) {
+                                                            double* partials, int pstride, MsN3Out o) {
     MS_SHARED_SETUP
-    for (int t = 0; t < MS_MOLS; ++t) {
-        const int64_t i = w * MS_MOLS + t;
-        if (i >= S.n) break;  // warp-uniform
-        const int ci = S.comp[i];
-        const SigDyn A{cP.comp[ci], ci};
-        auto pair = [&](int cj, const Real (*da_t)[3], const Real (*ea_t)[3], uint32_t jb, const Real* md, int fl,
-                        bool macro, Real eps, Real* fp, Real* mp, Real& u6p, Real& uxp, Real& rfp, MsCounts& n) {
-            const SigDyn B{cP.comp[cj], cj};
-            ms_molpair<Real>(A, B, da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, u6p, uxp, rfp, n);
-        };
-        ms_molecule<Real>(S, xlf, sd, se, sstride, nbr, nnb, maxnb, soff, ring[wl], site_i[wl], lane, i, A.ns(), epsRF,
-                          W, pair);
+    if constexpr (N3) {
+        __shared__ float sites[MS_WARPS][MS_MOLS][2][MD_MAXS][3];
+        __shared__ float acc[MS_WARPS][MS_MOLS][9];
+        const int64_t base = w * MS_MOLS;
+        const int nmol = (int)min((int64_t)MS_MOLS, S.n - base);
+        if (nmol > 0) {  // warp-uniform
+            auto pair = [&](int ci, int cj, const float (*da_t)[3], const float (*ea_t)[3], uint32_t jb, const float* md,
+                            int fl, bool macro, float eps, float* fp, float* mp, float* mq, float& u6p, float& uxp,
+                            float& rfp, MsCounts& n) {
+                const SigDyn A{cP.comp[ci], ci}, B{cP.comp[cj], cj};
+                ms_molpair<float, true>(A, B, da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, mq, u6p, uxp, rfp, n);
+            };
+            ms_warp_n3(S, xlf, sd, se, sstride, nbr, maxnb, soff, ring[wl], sites[wl], acc[wl], lane, base, nmol,
+                       epsRF, W, o, pair);
+        }
+    } else {
+        for (int t = 0; t < MS_MOLS; ++t) {
+            const int64_t i = w * MS_MOLS + t;
+            if (i >= S.n) break;  // warp-uniform
+            const int ci = S.comp[i];
+            const SigDyn A{cP.comp[ci], ci};
+            auto pair = [&](int cj, const Real (*da_t)[3], const Real (*ea_t)[3], uint32_t jb, const Real* md, int fl,
+                            bool macro, Real eps, Real* fp, Real* mp, Real* mq, Real& u6p, Real& uxp, Real& rfp,
+                            MsCounts& n) {
+                const SigDyn B{cP.comp[cj], cj};
+                ms_molpair<Real>(A, B, da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, mq, u6p, uxp, rfp, n);
+            };
+            ms_molecule<Real>(S, xlf, sd, se, sstride, nbr, nnb, maxnb, soff, ring[wl], site_i[wl], lane, i, A.ns(),
+                              epsRF, W, pair);
+        }
     }
     ms_store_partials<Real>(partials, pstride, W);
 }
@@ -1853,29 +2038,66 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOC
 // The same for a two-component system whose component signatures are S0 and
 // S1 at compile time (chosen at setup when the components match a compiled
 // pair of signatures): every molecule pair's site loops are straight code.
-template <typename Real, class S0, class S1>
-__global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? MS_MIN_BLOCKS : 3) k_force_ms2(State S, const float4* xlf, const Real* sd, const Real* se,
+template <typename Real, class S0, class S1, bool N3 = false>
+__global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? (N3 ? MS_N3_MIN_BLOCKS : MS_MIN_BLOCKS) : 3) k_force_ms2(State S, const float4* xlf, const Real* sd, const Real* se,
                                                              int stride, const uint32_t* nbr, const int* nnb, int maxnb,
-                                                             double* partials, int pstride) {
+                                                             double* partials, int pstride, MsN3Out o) {
     MS_SHARED_SETUP
-    for (int t = 0; t < MS_MOLS; ++t) {
-        const int64_t i = w * MS_MOLS + t;
-        if (i >= S.n) break;  // warp-uniform
-        const int ci = S.comp[i];
-        // one instance of the site-pair code per (home, neighbour) signature pair; the molecule-level code around
-        // it exists once
-        auto pair = [&](int cj, const Real (*da_t)[3], const Real (*ea_t)[3], uint32_t jb, const Real* md, int fl,
-                        bool macro, Real eps, Real* fp, Real* mp, Real& u6p, Real& uxp, Real& rfp, MsCounts& n) {
-            DispFix2<S0, S1>::run(ci, [&](auto A) {
-                DispFix2<S0, S1>::run(cj, [&](auto B) {
-                    ms_molpair<Real>(A, B, da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, u6p, uxp, rfp, n);
+    if constexpr (N3) {
+        __shared__ float sites[MS_WARPS][MS_MOLS][2][MD_MAXS][3];
+        __shared__ float acc[MS_WARPS][MS_MOLS][9];
+        const int64_t base = w * MS_MOLS;
+        const int nmol = (int)min((int64_t)MS_MOLS, S.n - base);
+        if (nmol > 0) {  // warp-uniform
+            auto pair = [&](int ci, int cj, const float (*da_t)[3], const float (*ea_t)[3], uint32_t jb, const float* md,
+                            int fl, bool macro, float eps, float* fp, float* mp, float* mq, float& u6p, float& uxp,
+                            float& rfp, MsCounts& n) {
+                DispFix2<S0, S1>::run(ci, [&](auto A) {
+                    DispFix2<S0, S1>::run(cj, [&](auto B) {
+                        ms_molpair<float, true>(A, B, da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, mq, u6p, uxp,
+                                                rfp, n);
+                    });
                 });
-            });
-        };
-        ms_molecule<Real>(S, xlf, sd, se, sstride, nbr, nnb, maxnb, soff, ring[wl], site_i[wl], lane, i,
-                          cP.comp[ci].ns, epsRF, W, pair);
+            };
+            ms_warp_n3(S, xlf, sd, se, sstride, nbr, maxnb, soff, ring[wl], sites[wl], acc[wl], lane, base, nmol,
+                       epsRF, W, o, pair);
+        }
+    } else {
+        for (int t = 0; t < MS_MOLS; ++t) {
+            const int64_t i = w * MS_MOLS + t;
+            if (i >= S.n) break;  // warp-uniform
+            const int ci = S.comp[i];
+            // one instance of the site-pair code per (home, neighbour) signature pair; the molecule-level code
+            // around it exists once
+            auto pair = [&](int cj, const Real (*da_t)[3], const Real (*ea_t)[3], uint32_t jb, const Real* md, int fl,
+                            bool macro, Real eps, Real* fp, Real* mp, Real* mq, Real& u6p, Real& uxp, Real& rfp,
+                            MsCounts& n) {
+                DispFix2<S0, S1>::run(ci, [&](auto A) {
+                    DispFix2<S0, S1>::run(cj, [&](auto B) {
+                        ms_molpair<Real>(A, B, da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, mq, u6p, uxp, rfp,
+                                         n);
+                    });
+                });
+            };
+            ms_molecule<Real>(S, xlf, sd, se, sstride, nbr, nnb, maxnb, soff, ring[wl], site_i[wl], lane, i,
+                              cP.comp[ci].ns, epsRF, W, pair);
+        }
     }
     ms_store_partials<Real>(partials, pstride, W);
+}
+
+// The Newton-3 form's accumulators added to the per-molecule outputs the pair
+// kernel stored (F, M, Vi of the molecule's own row) and cleared: FP32 values
+// converted exactly and added in FP64.
+__global__ void k_ms_n3_store(State S, MsN3Out o) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 a = o.f[i], b = o.m[i], c = o.v[i];
+    o.f[i] = z; o.m[i] = z; o.v[i] = z;
+    S.Fx[i] += f2d_exact(a.x); S.Fy[i] += f2d_exact(a.y); S.Fz[i] += f2d_exact(a.z);
+    S.Mx[i] += f2d_exact(b.x); S.My[i] += f2d_exact(b.y); S.Mz[i] += f2d_exact(b.z);
+    S.Vx[i] += f2d_exact(c.x); S.Vy[i] += f2d_exact(c.y); S.Vz[i] += f2d_exact(c.z);
 }
 
 // Signatures the two-component kernel is compiled for: the 2CLJQ + 1CLJD

@@ -93,11 +93,14 @@ def test_precision_and_pair_counts_at_full_size(mods, name):
     assert abs(fo6.virial - foo.virial) <= 1e-10 * abs(foo.virial)
 
 
-@pytest.mark.parametrize("name", ["C2a_lj4m", "C2b_slab3m"])
+@pytest.mark.parametrize("name", sorted(CONFIGS))
 def test_newton3_at_full_size(mods, name):
-    """The Newton-3 cluster-pair path at the 1CLJ benchmark sizes: the same
-    interacting pair counts as the FP64 kernel (exact), relative rms force
-    error <= 1e-5 and Upot, virial <= 1e-6 against it."""
+    """The Newton-3 paths at the benchmark sizes -- cluster pairs for the
+    1CLJ configurations, the multi-site kernels' half rows with atomics for
+    the mixture: the same interacting pair counts as the FP64 kernel
+    (exact), relative rms force error <= 1e-5 and Upot, virial, pressure
+    <= 1e-6 against it (mixture: torques <= 1e-4, sums <= 1e-5, the bars of
+    the rows above)."""
     E, psm, P = mods
     gen, rc, dt, skin, nsteps = CONFIGS[name]
     ps0 = gen(psm)
@@ -113,8 +116,11 @@ def test_newton3_at_full_size(mods, name):
     print(name, "newton3", rep)
     assert rep["pairs_equal"], rep
     assert rep["force_rel_rms"] <= 1e-5, rep
+    if "torque_rel_rms" in rep:
+        assert rep["torque_rel_rms"] <= 1e-4, rep
+    tol = 1e-5 if "torque_rel_rms" in rep else 1e-6
     for k in ("upot_rel", "virial_rel", "pressure_rel"):
-        assert rep[k] <= 1e-6, rep
+        assert rep[k] <= tol, rep
 
 
 def _drift(En):

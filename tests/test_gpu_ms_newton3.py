@@ -1,0 +1,125 @@
+"""The multi-site kernels' Newton-3 form (md_config.pair_scheme =
+MD_PAIRS_NEWTON3, mixed precision): every molecule pair is evaluated once,
+from the higher-slot part of the lower slot's candidate row, and the
+neighbour's force, torque and virial are added to FP32 accumulators by
+vector atomics (Newton's third law as the reference's processCellPair
+applies it, VectorizedCellProcessor.cpp:2744-2819).
+
+Bars:
+  * against the reference's golden outputs of every multi-site case (the
+    ten Vectorization inputs, nine of them multi-site, and the periodic
+    mixture): the mixed tolerances of the row kernels (relative rms force
+    error <= 1e-5, torques and virials <= 1e-4, Upot/virial 1e-5), site pair
+    counts exact;
+  * against the rows (every pair from both sides) on the same state:
+    molecule and site pair counts equal, F, M, Vi to 1e-5 relative rms (two
+    FP32 summation orders), Upot and virial to 1e-6 relative;
+  * the reference's NVE run of the rotating mixture (nve_mix500, 20 steps):
+    per-step Upot, virial, sum m v^2, sum I w^2 to 1e-4 relative, the mixed
+    NVE tolerance;
+  * md_adjoint on a Newton-3 context (its kernels walk the whole rows, whose
+    order the split changes) equals the rows context's to 1e-5.
+"""
+import numpy as np
+import pytest
+
+import golden_io
+
+pytestmark = pytest.mark.gpu
+
+
+def _multisite(ps):
+    return any(len(c.lj) != 1 or c.charges or c.dipoles or c.quadrupoles or any(x != 0 for x in c.lj[0].r)
+               for c in ps.components)
+
+
+MS_CASES = [n for n in golden_io.names("ref_") + golden_io.names("per_") if _multisite(golden_io.load(n)[0])]
+
+
+@pytest.fixture(scope="module")
+def E():
+    import importlib
+    import build as eb
+    eb.build()
+    return importlib.import_module("ls1gb300.engine")
+
+
+def _by_id(ids):
+    return np.argsort(ids, kind="stable")
+
+
+def _rel_rms(a, b):
+    return np.sqrt(((a - b) ** 2).sum(axis=1).mean()) / max(np.sqrt((b ** 2).sum(axis=1).mean()), 1e-300)
+
+
+def _run(E, ps, g, scheme):
+    e = E.Engine(ps, g["rc"], g["rc_lj"], (1, 1, 1) if g["periodic"] else (0, 0, 0), precision="mixed", skin=0.0,
+                 pair_scheme=scheme)
+    fo = e.forces()
+    m = e.molecules()
+    used = e.time_kernels(1).pair_scheme
+    return e, fo, m, used
+
+
+def test_the_multisite_cases_are_there():
+    assert len(MS_CASES) == 10 and "per_mix500" in MS_CASES
+
+
+@pytest.mark.parametrize("name", MS_CASES)
+def test_newton3_forces_match_reference_and_rows(E, name):
+    ps, g = golden_io.load(name)
+    e, fo, m, used = _run(E, ps, g, "newton3")
+    e.close()
+    assert used == 1
+    a, b = _by_id(m["ids"]), _by_id(g["out_ids"])
+    assert _rel_rms(m["F"][a], g["F"][b]) <= 1e-5
+    for key in ("M", "Vi"):
+        if np.abs(g[key]).max() > 1e-6:
+            assert _rel_rms(m[key][a], g[key][b]) <= 1e-4, key
+        else:
+            assert np.abs(m[key][a] - g[key][b]).max() < 1e-4, key
+    for mine, ref in ((fo.upot, float(g["upot"])), (fo.virial, float(g["virial"]))):
+        assert abs(mine - ref) <= 1e-5 * max(1.0, abs(ref))
+    assert list(fo.site_pairs) == list(g["counts"][2::2].astype(np.int64))
+    # the rows on the same state
+    er, fr, mr, used_r = _run(E, ps, g, "rows")
+    er.close()
+    assert used_r == 0
+    assert fo.mol_pairs == fr.mol_pairs and list(fo.site_pairs) == list(fr.site_pairs)
+    ia, ir = _by_id(m["ids"]), _by_id(mr["ids"])
+    for key in ("F", "M", "Vi"):
+        if np.abs(mr[key]).max() > 1e-6:
+            assert _rel_rms(m[key][ia], mr[key][ir]) <= 1e-5, key
+        else:
+            assert np.abs(m[key][ia] - mr[key][ir]).max() < 1e-6, key
+    assert abs(fo.upot - fr.upot) <= 1e-6 * abs(fr.upot)
+    assert abs(fo.virial - fr.virial) <= 1e-6 * max(abs(fr.virial), 1e-300)
+
+
+def test_newton3_nve_of_the_rotating_mixture(E):
+    ps, g = golden_io.load("nve_mix500")
+    e = E.Engine(ps, g["rc"], g["rc_lj"], (1, 1, 1), precision="mixed", skin=0.0, pair_scheme="newton3")
+    e.forces()
+    rec = e.run(float(g["dt"]), int(g["nsteps"]))
+    assert e.time_kernels(1).pair_scheme == 1
+    e.close()
+    ref = g["steps"][1:, 1:]
+    for col in range(4):
+        scale = max(np.abs(ref[:, col]).max(), 1e-300)
+        assert np.abs(rec[:, col] - ref[:, col]).max() <= 1e-4 * scale, col
+
+
+def test_adjoint_on_a_newton3_context_equals_the_rows(E):
+    ps, g = golden_io.load("per_mix500")
+    out = {}
+    for scheme in ("newton3", "rows"):
+        e, fo, m, used = _run(E, ps, g, scheme)
+        gr, gp = e.adjoint(1.0, 0.5)
+        e.close()
+        out[scheme] = (m["ids"], gr, gp, used)
+    assert out["newton3"][3] == 1 and out["rows"][3] == 0
+    ids3, gr3, gp3, _ = out["newton3"]
+    idsr, grr, gpr, _ = out["rows"]
+    np.testing.assert_array_equal(np.sort(ids3), np.sort(idsr))
+    assert _rel_rms(gr3[_by_id(ids3)], grr[_by_id(idsr)]) <= 1e-5
+    assert np.abs(gp3 - gpr).max() <= 1e-5 * np.abs(gpr).max()
