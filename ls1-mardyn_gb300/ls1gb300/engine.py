@@ -104,9 +104,11 @@ class Engine:
                  periodic: Sequence[int] = (1, 1, 1), precision: str = "fp64", skin: float = 0.0,
                  device: int = 0, capacity: int = 0, pair_scheme: str = "rows", arrays=None):
         """pair_scheme "rows": per-molecule candidate rows, each pair evaluated from both sides;
-        "newton3": every pair evaluated once (Newton's third law, cluster pairs) where the system allows
-        it (one component of single-centre LJ molecules, mixed precision), rows elsewhere.  arrays: the
-        molecule arrays of ``abi.molecule_arrays(ps)`` to upload (e.g. page-locked copies), else made from ps."""
+        "newton3": every pair evaluated once (Newton's third law) in mixed precision where the box has
+        at least three list cells per periodic axis -- cluster pairs for one component of single-centre
+        LJ molecules, half rows with the neighbour's share added by atomics for multi-site molecules --
+        rows elsewhere.  arrays: the molecule arrays of ``abi.molecule_arrays(ps)`` to upload (e.g.
+        page-locked copies), else made from ps."""
         self.L = load_library()
         self.ps = ps
         self.cfg = abi.make_config(ps.box, rc, rc if rc_lj is None else rc_lj, ps.eps_rf, periodic,

@@ -17,8 +17,9 @@ Bars:
   * the reference's NVE run of the rotating mixture (nve_mix500, 20 steps):
     per-step Upot, virial, sum m v^2, sum I w^2 to 1e-4 relative, the mixed
     NVE tolerance;
-  * md_adjoint on a Newton-3 context (its kernels walk the whole rows, whose
-    order the split changes) equals the rows context's to 1e-5.
+  * md_adjoint on a Newton-3 context (its own Newton-3 kernel: each pair
+    once, the neighbour's position gradient by atomics) equals the rows
+    context's to 1e-5, with and without a force cotangent.
 """
 import numpy as np
 import pytest
@@ -109,17 +110,27 @@ def test_newton3_nve_of_the_rotating_mixture(E):
         assert np.abs(rec[:, col] - ref[:, col]).max() <= 1e-4 * scale, col
 
 
-def test_adjoint_on_a_newton3_context_equals_the_rows(E):
-    ps, g = golden_io.load("per_mix500")
+@pytest.mark.parametrize("with_gF", [False, True])
+@pytest.mark.parametrize("name", ["per_mix500", "ref_VectorizationDipoleQuadrupole",
+                                  "ref_VectorizationMultiComponentMultiPotentials"])
+def test_adjoint_on_a_newton3_context_equals_the_rows(E, name, with_gF):
+    """md_adjoint on a Newton-3 context runs its Newton-3 kernel (each pair
+    once, the neighbour's share by atomics): the same position and
+    parameter gradients as the rows context's adjoint (every pair from both
+    sides) to 1e-5 -- with and without a force cotangent gF (the dual-number
+    and the homogeneity instances), for the two-component kernel and the
+    general one."""
+    ps, g = golden_io.load(name)
+    gF = np.random.default_rng(3).normal(size=(ps.n, 3)) if with_gF else None
     out = {}
     for scheme in ("newton3", "rows"):
         e, fo, m, used = _run(E, ps, g, scheme)
-        gr, gp = e.adjoint(1.0, 0.5)
+        gr, gp = e.adjoint(1.0, 0.5, gF)
         e.close()
-        out[scheme] = (m["ids"], gr, gp, used)
-    assert out["newton3"][3] == 1 and out["rows"][3] == 0
-    ids3, gr3, gp3, _ = out["newton3"]
-    idsr, grr, gpr, _ = out["rows"]
-    np.testing.assert_array_equal(np.sort(ids3), np.sort(idsr))
-    assert _rel_rms(gr3[_by_id(ids3)], grr[_by_id(idsr)]) <= 1e-5
+        out[scheme] = (gr, gp, used)
+    assert out["newton3"][2] == 1 and out["rows"][2] == 0
+    gr3, gp3, _ = out["newton3"]
+    grr, gpr, _ = out["rows"]
+    # grad_r is in upload order in both contexts
+    assert _rel_rms(gr3, grr) <= 1e-5
     assert np.abs(gp3 - gpr).max() <= 1e-5 * np.abs(gpr).max()
