@@ -809,11 +809,11 @@ def main():
     if a.workload == "lj4m" and a.precision == "mixed" and not rmm:
         mps = psm.with_vacancies(psm.mixture(108_000, 18.0, 300.0, seed=4), 100_000, 18.0, 4)
         ktm = {}
-        for scheme in ("rows", "newton3"):
-            em = E.Engine(mps, 1.0, precision="mixed", skin=0.1, device=local, pair_scheme=scheme)
+        for mscheme in ("rows", "newton3"):
+            em = E.Engine(mps, 1.0, precision="mixed", skin=0.1, device=local, pair_scheme=mscheme)
             em.forces()
             em.run(9.118e-5, 200, record=False)  # off the lattice, as the differentiation workload's snapshots
-            ktm[scheme] = em.time_kernels(5)
+            ktm[mscheme] = em.time_kernels(5)
             em.close()
         adj_mix = {"system": f"2CLJQ/1CLJD mixture, {mps.n:,} molecules, n=18 nm^-3, T=300 K, rc=1 nm, after 200 steps",
                    "kernel_forward_ms": ktm["rows"].force_ms, "kernel_adjoint_ms": ktm["rows"].adjoint_ms,

@@ -1554,9 +1554,19 @@ static_assert(MD_SITE_VEC * MD_MAXS <= 32, "one lane per element loads the warp 
 #ifndef MS_ADJ_MIN_BLOCKS
 #define MS_ADJ_MIN_BLOCKS 5  // FP32 adjoint kernel: the same (96 registers, no spills)
 #endif
+#ifndef MS_ADJ_N3_MIN_BLOCKS
+// FP32 Newton-3 adjoint kernel: 72 registers, spills of 8-128 bytes per instance; measured on the
+// 100,000-molecule mixture 0.559 ms against 0.579 ms at 6 blocks (80 registers) and 0.633 ms at 5 (96)
+#define MS_ADJ_N3_MIN_BLOCKS 7
+#endif
 #define MS_ADJ_MIN_MOLS 8  // fewest molecules per warp of the multi-site adjoint
 #ifndef MS_N3_MIN_BLOCKS
-#define MS_N3_MIN_BLOCKS 5  // FP32 Newton-3 force kernel: the same (96 registers, no spills)
+#define MS_N3_MIN_BLOCKS 5  // FP32 Newton-3 force kernel, general signatures: the same (96 registers, no spills)
+#endif
+#ifndef MS2_N3_MIN_BLOCKS
+// FP32 Newton-3 two-component kernel: 72 registers, a 16-byte spill; measured at the 1M mixture 1.59 ms
+// against 1.63 ms at 6 blocks (80 registers), 1.75 ms at 5 (92) and more spills at 8
+#define MS2_N3_MIN_BLOCKS 7
 #endif
 
 // Site signature of a component as the multi-site kernels read it (sites in
@@ -1873,17 +1883,18 @@ __device__ __forceinline__ void ms_store_partials(double* partials, int pstride,
 // one molecule's neighbours would leave most of its last group of 32 lanes
 // idle; the ring of in-cut-off candidates therefore runs on across the warp's
 // molecules, each entry tagged with its home molecule t (site records of all
-// of them staged in shared memory, sites[t]), and every group of 32 lanes
+// of them staged in shared memory, sites[t]: NSM sites, the most of any
+// component the kernel serves), and every group of 32 lanes
 // evaluates 32 molecule pairs of one or several homes.  The home's share of a
 // group (F, M, m_d o F) is summed per home by a segmented warp scan (the tags
 // of a group are contiguous and ascending) and added by the segment's last
 // lane to the home's shared accumulator acc[t]; the neighbour's share goes to
 // its global accumulators in o.  `pair(ci, cj, ...)` evaluates one molecule
 // pair as in ms_molecule.
-template <class Pair>
+template <int NSM, class Pair>
 __device__ __forceinline__ void ms_warp_n3(const State& S, const float4* xlf, const float* sd, const float* se,
                                            uint32_t sstride, const uint32_t* nbr, int maxnb,
-                                           const float (*soff)[3], uint32_t* ring, float (*sites)[2][MD_MAXS][3],
+                                           const float (*soff)[3], uint32_t* ring, float (*sites)[2][NSM][3],
                                            float (*acc)[9], int lane, int64_t base, int nmol, float epsRF,
                                            MsWarp<float>& W, MsN3Out o, Pair pair) {
     const unsigned FULL = 0xffffffffu;
@@ -1891,7 +1902,7 @@ __device__ __forceinline__ void ms_warp_n3(const State& S, const float4* xlf, co
     __syncwarp();
     for (uint32_t k = lane; k < (uint32_t)nmol * sstride; k += 32) {
         const uint32_t t = k / sstride, r = k % sstride, a = r / MD_SITE_VEC, c = r % MD_SITE_VEC;
-        if (c < 3 && a < MD_MAXS) {
+        if (c < 3 && a < NSM) {
             sites[t][0][a][c] = sd[(uint32_t)base * sstride + k];
             sites[t][1][a][c] = se[(uint32_t)base * sstride + k];
         }
@@ -2013,7 +2024,7 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? (N3 ? MS_N3
                 const SigDyn A{cP.comp[ci], ci}, B{cP.comp[cj], cj};
                 ms_molpair<float, true>(A, B, da_t, ea_t, sd, se, jb, md, fl, macro, eps, fp, mp, mq, u6p, uxp, rfp, n);
             };
-            ms_warp_n3(S, xlf, sd, se, sstride, nbr, maxnb, soff, ring[wl], sites[wl], acc[wl], lane, base, nmol,
+            ms_warp_n3<MD_MAXS>(S, xlf, sd, se, sstride, nbr, maxnb, soff, ring[wl], sites[wl], acc[wl], lane, base, nmol,
                        epsRF, W, o, pair);
         }
     } else {
@@ -2039,12 +2050,13 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? (N3 ? MS_N3
 // S1 at compile time (chosen at setup when the components match a compiled
 // pair of signatures): every molecule pair's site loops are straight code.
 template <typename Real, class S0, class S1, bool N3 = false>
-__global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? (N3 ? MS_N3_MIN_BLOCKS : MS_MIN_BLOCKS) : 3) k_force_ms2(State S, const float4* xlf, const Real* sd, const Real* se,
+__global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? (N3 ? MS2_N3_MIN_BLOCKS : MS_MIN_BLOCKS) : 3) k_force_ms2(State S, const float4* xlf, const Real* sd, const Real* se,
                                                              int stride, const uint32_t* nbr, const int* nnb, int maxnb,
                                                              double* partials, int pstride, MsN3Out o) {
     MS_SHARED_SETUP
     if constexpr (N3) {
-        __shared__ float sites[MS_WARPS][MS_MOLS][2][MD_MAXS][3];
+        constexpr int NSM = S0::ns() > S1::ns() ? S0::ns() : S1::ns();
+        __shared__ float sites[MS_WARPS][MS_MOLS][2][NSM][3];
         __shared__ float acc[MS_WARPS][MS_MOLS][9];
         const int64_t base = w * MS_MOLS;
         const int nmol = (int)min((int64_t)MS_MOLS, S.n - base);
@@ -2059,7 +2071,7 @@ __global__ void __launch_bounds__(MS_WARPS * 32, sizeof(Real) == 4 ? (N3 ? MS_N3
                     });
                 });
             };
-            ms_warp_n3(S, xlf, sd, se, sstride, nbr, maxnb, soff, ring[wl], sites[wl], acc[wl], lane, base, nmol,
+            ms_warp_n3<NSM>(S, xlf, sd, se, sstride, nbr, maxnb, soff, ring[wl], sites[wl], acc[wl], lane, base, nmol,
                        epsRF, W, o, pair);
         }
     } else {
