@@ -19,7 +19,10 @@ Bars:
     NVE tolerance;
   * md_adjoint on a Newton-3 context (its own Newton-3 kernel: each pair
     once, the neighbour's position gradient by atomics) equals the rows
-    context's to 1e-5, with and without a force cotangent.
+    context's to 1e-5, with and without a force cotangent;
+  * edge cases against the oracle (one molecule, a pair across the periodic
+    boundary, a dilute gas, a dense block in a corner of a large box and in
+    a closed box): pair counts exact, forces 1e-5 rms, torques 1e-4.
 """
 import numpy as np
 import pytest
@@ -134,3 +137,70 @@ def test_adjoint_on_a_newton3_context_equals_the_rows(E, name, with_gF):
     # grad_r is in upload order in both contexts
     assert _rel_rms(gr3, grr) <= 1e-5
     assert np.abs(gp3 - gpr).max() <= 1e-5 * np.abs(gpr).max()
+
+
+def _subset(ps0, idx, box, r):
+    """Molecules idx of ps0 at positions r in a box of edge box."""
+    q = ps0.copy()
+    idx = np.asarray(idx)
+    q.box = np.array([box, box, box], float)
+    q.ids, q.comp = ps0.ids[idx].copy(), ps0.comp[idx].copy()
+    q.r = np.asarray(r, float).reshape(len(idx), 3)
+    q.v, q.q, q.L = ps0.v[idx].copy(), ps0.q[idx].copy(), ps0.L[idx].copy()
+    return q
+
+
+def _edge_cases():
+    from ls1gb300 import phasespace as psm
+    ps0 = psm.mixture(500, 18.0, 300.0, seed=9)
+    a0, b0 = int(np.flatnonzero(ps0.comp == 0)[0]), int(np.flatnonzero(ps0.comp == 1)[0])
+    rng = np.random.default_rng(17)
+    pts = []
+    while len(pts) < 40:
+        p = rng.uniform(0, 10.0, 3)
+        if all(np.linalg.norm(((p - q) + 5.0) % 10.0 - 5.0) > 0.6 for q in pts):
+            pts.append(p)
+    return {
+        "single": (_subset(ps0, [a0], 4.0, [[2.0, 2.0, 2.0]]), (1, 1, 1)),
+        # an A and a B molecule 0.55 nm apart across the periodic boundary
+        "pair_across_boundary": (_subset(ps0, [a0, b0], 4.0, [[0.2, 2.0, 2.0], [3.65, 2.05, 1.95]]), (1, 1, 1)),
+        # 40 molecules in a 10 nm box: mostly empty cells, most half rows empty
+        "dilute": (_subset(ps0, np.arange(40), 10.0, pts), (1, 1, 1)),
+        # the 500-molecule block in a corner of a 9 nm box, wrapped across the boundary: long rows
+        "corner_cluster": (_subset(ps0, np.arange(ps0.n), 9.0, np.mod(ps0.r - 1.0, 9.0)), (1, 1, 1)),
+        # the same block in a closed (non-periodic) box
+        "closed_box": (_subset(ps0, np.arange(ps0.n), 6.5, ps0.r + 1.5), (0, 0, 0)),
+    }
+
+
+EDGE = sorted(_edge_cases())
+
+
+@pytest.mark.parametrize("name", EDGE)
+def test_newton3_edge_cases_against_the_oracle(E, name):
+    """Edge cases of the half rows and the cross-molecule ring against the
+    oracle (FP64, the reference's algorithm): one molecule, a pair across
+    the periodic boundary, a dilute gas (most half rows empty, warps with
+    few in-cut-off pairs), a dense block in one corner of a large box (long
+    rows) and in a closed box.  Pair counts exact, relative rms force error
+    <= 1e-5, torques <= 1e-4, Upot and virial <= 1e-5 relative."""
+    from oracle.oracle import Oracle
+    ps, per = _edge_cases()[name]
+    e = E.Engine(ps, 1.0, 1.0, per, precision="mixed", skin=0.3, pair_scheme="newton3")
+    fo = e.forces()
+    m = e.molecules()
+    assert e.time_kernels(1).pair_scheme == 1
+    e.close()
+    o = Oracle(ps, 1.0, 1.0, per)
+    o.rebin()
+    foo, _ = o.forces()
+    mo = o.molecules()
+    assert fo.mol_pairs == foo.mol_pairs and list(fo.site_pairs) == list(foo.site_pairs)
+    a, b = _by_id(m["ids"]), _by_id(mo["ids"])
+    for key, tol in (("F", 1e-5), ("M", 1e-4)):
+        if np.abs(mo[key]).max() > 0:
+            assert _rel_rms(m[key][a], mo[key][b]) <= tol, key
+        else:
+            assert np.abs(m[key]).max() == 0.0, key
+    for mine, ref in ((fo.upot, foo.upot), (fo.virial, foo.virial)):
+        assert abs(mine - ref) <= 1e-5 * max(abs(ref), 1e-300) or (ref == 0.0 and mine == 0.0)
