@@ -41,8 +41,11 @@ void GpuLinkedCells::readXML(XMLfileUnits& xmlconfig) {
 	_precision = (prec == "fp64") ? MD_PREC_FP64 : MD_PREC_MIXED;
 	xmlconfig.getNodeValueReduced("skin", _skin);
 	xmlconfig.getNodeValue("device", _device);
+	std::string scheme = "rows";
+	xmlconfig.getNodeValue("pairscheme", scheme);
+	_pairScheme = (scheme == "newton3") ? MD_PAIRS_NEWTON3 : MD_PAIRS_ROWS;
 	Log::global_log->info() << "GpuLinkedCells: precision " << prec << ", skin " << _skin << ", device " << _device
-							<< std::endl;
+							<< ", pair scheme " << scheme << std::endl;
 }
 
 void GpuLinkedCells::update() {
@@ -74,6 +77,7 @@ void GpuLinkedCells::ensureDevice() {
 		cfg.precision = _precision;
 		cfg.skin = _skin;
 		cfg.device = _device;
+		cfg.pair_scheme = _pairScheme;
 		check(md_create(&_ctx, &cfg), "md_create");
 		// components and Lorentz-Berthelot coefficients (Comp2Param::initialize inputs)
 		std::vector<Component>& comps = *(global_simulation->getEnsemble()->getComponents());

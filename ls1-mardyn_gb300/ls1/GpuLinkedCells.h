@@ -79,6 +79,7 @@ private:
 	int _precision = MD_PREC_MIXED;
 	double _skin = 0.3;
 	int _device = 0;
+	int _pairScheme = MD_PAIRS_ROWS;  // <pairscheme>rows|newton3</pairscheme>
 	double _rc = 0.0, _rcLJ = 0.0;
 	bool _hostStale = false;    // device state ahead of the host mirror
 	bool _deviceStale = true;   // host mirror edited since the last upload
