@@ -38,6 +38,7 @@ struct CompDev {
     double m, I[3], invI[3];
     double d[MD_MAXS][3];   // body-frame site offsets, order LJ, charges, dipoles, quadrupoles
     double e[MD_MAXS][3];   // body-frame orientations (dipoles/quadrupoles)
+    float df[MD_MAXS][3], ef[MD_MAXS][3];  // the same rounded to FP32 (the mixed-precision site caches)
     double p[MD_MAXS];      // q, |mu| or |Q|
     int kind[MD_MAXS];
     int zero_offset[MD_MAXS];
@@ -125,6 +126,17 @@ __device__ __forceinline__ void qrot(double w, double x, double y, double z, con
     o[0] = (ww + xx - yy - zz) * d[0] + 2. * (xy - wz) * d[1] + 2. * (wy + xz) * d[2];
     o[1] = 2. * (wz + xy) * d[0] + (ww - xx + yy - zz) * d[1] + 2. * (yz - wx) * d[2];
     o[2] = 2. * (xz - wy) * d[0] + 2. * (wx + yz) * d[1] + (ww - xx - yy + zz) * d[2];
+}
+
+// The same rotation in FP32, for the mixed-precision site caches (the pair
+// arithmetic's precision).
+__device__ __forceinline__ void qrotf(float w, float x, float y, float z, const float* d, float* o) {
+    if (d[0] == 0.f && d[1] == 0.f && d[2] == 0.f) { o[0] = o[1] = o[2] = 0.f; return; }
+    float ww = w * w, xx = x * x, yy = y * y, zz = z * z;
+    float wx = w * x, wy = w * y, wz = w * z, xy = x * y, xz = x * z, yz = y * z;
+    o[0] = (ww + xx - yy - zz) * d[0] + 2.f * (xy - wz) * d[1] + 2.f * (wy + xz) * d[2];
+    o[1] = 2.f * (wz + xy) * d[0] + (ww - xx + yy - zz) * d[1] + 2.f * (yz - wx) * d[2];
+    o[2] = 2.f * (xz - wy) * d[0] + 2.f * (wx + yz) * d[1] + (ww - xx - yy + zz) * d[2];
 }
 
 // Quaternion::rotateinv (Quaternion.cpp:66-90)

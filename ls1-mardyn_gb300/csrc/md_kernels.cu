@@ -820,6 +820,21 @@ __global__ void k_sites(State S, Real* sd, Real* se, int stride) {
     double s = 1. / sqrt(w * w + x * x + y * y + z * z);
     w *= s; x *= s; y *= s; z *= s;
     S.qw[i] = w; S.qx[i] = x; S.qy[i] = y; S.qz[i] = z;
+    if (sizeof(Real) == 4) {
+        // FP32 caches: the rotation in FP32 from the normalised FP64 quaternion (rounded on the integer pipes;
+        // GB300's FP64 rate made the FP64 rotations most of this kernel's time)
+        const float wf = d2f_int(w), xf = d2f_int(x), yf = d2f_int(y), zf = d2f_int(z);
+        for (int k = 0; k < C.ns; ++k) {
+            float o[3];
+            qrotf(wf, xf, yf, zf, C.df[k], o);
+            for (int e = 0; e < 3; ++e) sd[((int64_t)i * stride + k) * MD_SITE_VEC + e] = (Real)o[e];
+            if (C.kind[k] >= SK_DIPOLE) {
+                qrotf(wf, xf, yf, zf, C.ef[k], o);
+                for (int e = 0; e < 3; ++e) se[((int64_t)i * stride + k) * MD_SITE_VEC + e] = (Real)o[e];
+            }
+        }
+        return;
+    }
     for (int k = 0; k < C.ns; ++k) {
         double o[3];
         qrot(w, x, y, z, C.d[k], o);
