@@ -817,7 +817,9 @@ __global__ void k_sites(State S, Real* sd, Real* se, int stride) {
     if (i >= S.n) return;
     const CompDev& C = cP.comp[S.comp[i]];
     double w = S.qw[i], x = S.qx[i], y = S.qy[i], z = S.qz[i];
-    double s = 1. / sqrt(w * w + x * x + y * y + z * z);
+    // (CUDA's FP64 rsqrt: within an ulp of 1 / sqrt, one call where sqrt and a division each take several FP64
+    // instructions on GB300's slow FP64 pipe; the reference divides by the norm, which rounds differently anyway)
+    double s = rsqrt(w * w + x * x + y * y + z * z);
     w *= s; x *= s; y *= s; z *= s;
     S.qw[i] = w; S.qx[i] = x; S.qy[i] = y; S.qz[i] = z;
     if (sizeof(Real) == 4) {
@@ -1383,6 +1385,7 @@ __global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __res
 // warp per molecule; the row is staged in dynamic shared memory, maxnb
 // entries per warp).  Only the order within a row changes.
 #define ROW_PART_SMEM (48 * 1024)  // shared bytes per block of k_row_partition (rows staged whole)
+#define ROW_PART_BYTES(maxnb) ((int64_t)(maxnb) * 5)  // per row: the entries and a one-byte part key each
 
 // With nhalf (the multi-site kernels' Newton-3 form) each row is first split
 // into the neighbours in higher slots and those in lower slots, each part
@@ -1395,25 +1398,28 @@ __global__ void k_row_partition(int64_t n, const float4* __restrict__ xl, uint32
     const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + wl;
     if (i >= n) return;  // warp-uniform
     uint32_t* buf = rowbuf + (size_t)wl * maxnb;
+    // each entry's part (lower half x ncomp + the neighbour's component), found once
+    uint8_t* key = reinterpret_cast<uint8_t*>(rowbuf + (size_t)(blockDim.x >> 5) * maxnb) + (size_t)wl * maxnb;
     uint32_t* row = nbr + (size_t)i * maxnb;
     const int cnt = nnb[i];
-    for (int k = lane; k < cnt; k += 32) buf[k] = row[k];
+    for (int k = lane; k < cnt; k += 32) {
+        const uint32_t e = row[k];
+        const int64_t j = e & MD_INDEX_MASK;
+        const int c = ncomp == 1 ? 0 : __float_as_int(__ldg(&xl[j]).w);
+        buf[k] = e;
+        key[k] = (uint8_t)((nhalf && j < i ? ncomp : 0) + c);
+    }
     __syncwarp();
     int out = 0;
     const int parts = nhalf ? 2 : 1;
     for (int h = 0; h < parts; ++h) {
         for (int c = 0; c < ncomp; ++c) {
+            const int want = h * ncomp + c;
             for (int k0 = 0; k0 < cnt; k0 += 32) {
                 const int k = k0 + lane;
-                uint32_t e = 0u;
-                bool m = false;
-                if (k < cnt) {
-                    e = buf[k];
-                    const int64_t j = e & MD_INDEX_MASK;
-                    m = (ncomp == 1 || __float_as_int(__ldg(&xl[j]).w) == c) && (!nhalf || (j > i) == (h == 0));
-                }
+                const bool m = k < cnt && key[k] == want;
                 const unsigned bal = __ballot_sync(0xffffffffu, m);
-                if (m) row[out + __popc(bal & ((1u << lane) - 1u))] = e;
+                if (m) row[out + __popc(bal & ((1u << lane) - 1u))] = buf[k];
                 out += __popc(bal);
             }
         }
@@ -2165,7 +2171,7 @@ __global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const 
             qh[2] = .5 * (q[3] * w[0] + q[0] * w[1] - q[1] * w[2]);
             qh[3] = .5 * (-q[2] * w[0] + q[1] * w[1] + q[0] * w[2]);
             for (int e = 0; e < 4; ++e) qh[e] = qh[e] * dt_halve + q[e];
-            double qc = 1. / sqrt(qh[0] * qh[0] + qh[1] * qh[1] + qh[2] * qh[2] + qh[3] * qh[3]);
+            double qc = rsqrt(qh[0] * qh[0] + qh[1] * qh[1] + qh[2] * qh[2] + qh[3] * qh[3]);  // as in k_sites
             for (int e = 0; e < 4; ++e) qh[e] *= qc;
             L[0] += dt_halve * S.Mx[i]; L[1] += dt_halve * S.My[i]; L[2] += dt_halve * S.Mz[i];
             qrotinv(qh[0], qh[1], qh[2], qh[3], L, w);
@@ -2176,7 +2182,7 @@ __global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const 
             qi[2] = .5 * (qh[3] * w[0] + qh[0] * w[1] - qh[1] * w[2]);
             qi[3] = .5 * (-qh[2] * w[0] + qh[1] * w[1] + qh[0] * w[2]);
             for (int e = 0; e < 4; ++e) q[e] += qi[e] * dt;
-            qc = 1. / sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+            qc = rsqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
             for (int e = 0; e < 4; ++e) q[e] *= qc;
             S.qw[i] = q[0]; S.qx[i] = q[1]; S.qy[i] = q[2]; S.qz[i] = q[3];
             S.Lx[i] = L[0]; S.Ly[i] = L[1]; S.Lz[i] = L[2];
