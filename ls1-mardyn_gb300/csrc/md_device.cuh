@@ -39,6 +39,7 @@ struct CompDev {
     double d[MD_MAXS][3];   // body-frame site offsets, order LJ, charges, dipoles, quadrupoles
     double e[MD_MAXS][3];   // body-frame orientations (dipoles/quadrupoles)
     float df[MD_MAXS][3], ef[MD_MAXS][3];  // the same rounded to FP32 (the mixed-precision site caches)
+    float If[3], invIf[3];                  // I and 1/I rounded to FP32 (mixed-precision rotational energy)
     double p[MD_MAXS];      // q, |mu| or |Q|
     int kind[MD_MAXS];
     int zero_offset[MD_MAXS];
@@ -147,6 +148,16 @@ __device__ __forceinline__ void qrotinv(double w, double x, double y, double z, 
     o[0] = (ww + xx - yy - zz) * d[0] + 2. * (xy + wz) * d[1] + 2. * (xz - wy) * d[2];
     o[1] = 2. * (xy - wz) * d[0] + (ww - xx + yy - zz) * d[1] + 2. * (yz + wx) * d[2];
     o[2] = 2. * (xz + wy) * d[0] + 2. * (yz - wx) * d[1] + (ww - xx - yy + zz) * d[2];
+}
+
+// Quaternion::rotateinv in FP32 (the mixed-precision rotational energy).
+__device__ __forceinline__ void qrotinvf(float w, float x, float y, float z, const float* d, float* o) {
+    if (d[0] == 0.f && d[1] == 0.f && d[2] == 0.f) { o[0] = o[1] = o[2] = 0.f; return; }
+    float ww = w * w, xx = x * x, yy = y * y, zz = z * z;
+    float wx = w * x, wy = w * y, wz = w * z, xy = x * y, xz = x * z, yz = y * z;
+    o[0] = (ww + xx - yy - zz) * d[0] + 2.f * (xy + wz) * d[1] + 2.f * (xz - wy) * d[2];
+    o[1] = 2.f * (xy - wz) * d[0] + (ww - xx + yy - zz) * d[1] + 2.f * (yz + wx) * d[2];
+    o[2] = 2.f * (xz + wy) * d[0] + 2.f * (yz - wx) * d[1] + (ww - xx - yy + zz) * d[2];
 }
 
 // Neighbouring doubles (IEEE successor / predecessor of a finite value), the

@@ -2286,6 +2286,10 @@ __global__ void k_sum_int(const int* a, int64_t n, unsigned long long* out) {
 }
 
 // FullMolecule::upd_postF with the Leapfrog sums.
+// With MIXED the rotational energy I w^2 (an observable: the state update is
+// FP64 either way) comes from an FP32 w = I^-1 R(q)^T L, as the fused
+// single-centre steps form their kinetic terms in FP32.
+template <bool MIXED>
 __global__ void k_post(State S, Kick K, double* partials, int pstride, int percomp) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double mv2 = 0.0, iw2 = 0.0;
@@ -2306,11 +2310,22 @@ __global__ void k_post(State S, Kick K, double* partials, int pstride, int perco
         if (!C.skip_rot) {  // L and M are only read for molecules that rotate
             double L[3] = {S.Lx[i] + dt_halve * S.Mx[i], S.Ly[i] + dt_halve * S.My[i], S.Lz[i] + dt_halve * S.Mz[i]};
             S.Lx[i] = L[0]; S.Ly[i] = L[1]; S.Lz[i] = L[2];
-            double w[3];
-            qrotinv(S.qw[i], S.qx[i], S.qy[i], S.qz[i], L, w);
-            for (int d = 0; d < 3; ++d) {
-                w[d] *= C.invI[d];
-                iw2 += C.I[d] * w[d] * w[d];
+            if (MIXED) {
+                const float Lf[3] = {d2f_int(L[0]), d2f_int(L[1]), d2f_int(L[2])};
+                float w[3], e = 0.f;
+                qrotinvf(d2f_int(S.qw[i]), d2f_int(S.qx[i]), d2f_int(S.qy[i]), d2f_int(S.qz[i]), Lf, w);
+                for (int d = 0; d < 3; ++d) {
+                    w[d] *= C.invIf[d];
+                    e += C.If[d] * w[d] * w[d];
+                }
+                iw2 = f2d_exact(e);
+            } else {
+                double w[3];
+                qrotinv(S.qw[i], S.qx[i], S.qy[i], S.qz[i], L, w);
+                for (int d = 0; d < 3; ++d) {
+                    w[d] *= C.invI[d];
+                    iw2 += C.I[d] * w[d] * w[d];
+                }
             }
         }
     }
