@@ -2163,7 +2163,8 @@ __global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const 
             double q[4] = {S.qw[i], S.qx[i], S.qy[i], S.qz[i]};
             double L[3] = {S.Lx[i], S.Ly[i], S.Lz[i]};
             double w[3];
-            qrotinv(q[0], q[1], q[2], q[3], L, w);
+            // q is a unit quaternion here (normalised at the end of the last step and by k_sites), as is qh below
+            qrotinv_unit(q[0], q[1], q[2], q[3], L, w);
             for (int d = 0; d < 3; ++d) w[d] *= C.invI[d];
             double qh[4];
             qh[0] = .5 * (-q[1] * w[0] - q[2] * w[1] - q[3] * w[2]);
@@ -2174,7 +2175,7 @@ __global__ void k_pre(State S, Kick K, float4* xlf, const double* origin, const 
             double qc = rsqrt(qh[0] * qh[0] + qh[1] * qh[1] + qh[2] * qh[2] + qh[3] * qh[3]);  // as in k_sites
             for (int e = 0; e < 4; ++e) qh[e] *= qc;
             L[0] += dt_halve * S.Mx[i]; L[1] += dt_halve * S.My[i]; L[2] += dt_halve * S.Mz[i];
-            qrotinv(qh[0], qh[1], qh[2], qh[3], L, w);
+            qrotinv_unit(qh[0], qh[1], qh[2], qh[3], L, w);
             for (int d = 0; d < 3; ++d) w[d] *= C.invI[d];
             double qi[4];
             qi[0] = .5 * (-qh[1] * w[0] - qh[2] * w[1] - qh[3] * w[2]);
