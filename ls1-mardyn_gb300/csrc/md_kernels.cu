@@ -373,8 +373,10 @@ __device__ void wrap_molecule(State& S, int64_t i, unsigned* status, unsigned lo
 __global__ void k_list_hist(State S, int* mcell, int* counts, unsigned* status, unsigned long long* nwrapped,
                             const unsigned* need, unsigned char* msub) {
     if (!*need) return;
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= S.n) return;
+    // grid-stride (as the other rebuild kernels): a step that needs no rebuild launches few blocks to skip; not
+    // unrolled, so that the registers stay those of one molecule per thread
+#pragma unroll 1
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S.n; i += (int64_t)gridDim.x * blockDim.x) {
     const double x = S.rx[i], y = S.ry[i], z = S.rz[i];
     if (!(x >= cP.bmin[0] && x < cP.bmax[0] && y >= cP.bmin[1] && y < cP.bmax[1] && z >= cP.bmin[2] && z < cP.bmax[2]))
         wrap_molecule(S, i, status, nwrapped);
@@ -389,6 +391,7 @@ __global__ void k_list_hist(State S, int* mcell, int* counts, unsigned* status, 
         for (int d = 0; d < 3; ++d)
             if ((r[d] - cP.bmin[d]) * cP.linv[d] - o[d] >= 0.5) k |= (unsigned char)(1u << d);
         msub[i] = k;
+    }
     }
 }
 
@@ -465,10 +468,11 @@ __global__ void k_scan3(const int* counts, int n, const int* boff, int* start, i
 
 __global__ void k_list_scatter(int64_t n, const int* mcell, int* cursor, int* perm, const unsigned* need) {
     if (!*need) return;
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int p = atomicAdd(&cursor[mcell[i]], 1);
-    perm[p] = (int)i;
+#pragma unroll 1
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int p = atomicAdd(&cursor[mcell[i]], 1);
+        perm[p] = (int)i;
+    }
 }
 
 // Deterministic order inside each cell: one warp per cell ranks the cell's
@@ -483,12 +487,23 @@ __device__ __forceinline__ int cell_sort_key(const int* comp, const unsigned cha
     return comp ? (comp[v] << MD_CODE_SHIFT) | v : (msub ? ((int)msub[v] << MD_CODE_SHIFT) | v : v);
 }
 
+__device__ __forceinline__ void cell_sort_one(const int* start, int* perm, const int* comp,
+                                              const unsigned char* msub, int c, int lane);
 __global__ void k_cell_sort(const int* start, int ncells, int* perm, const int* comp, const unsigned* need,
                             const unsigned char* msub) {
     if (!*need) return;
-    int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (c >= ncells) return;
+    const int lane = threadIdx.x & 31;
+    const int nw = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
+#pragma unroll 1
+    for (int c = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5); c < ncells; c += nw) {
+        cell_sort_one(start, perm, comp, msub, c, lane);
+        __syncwarp();  // (lane 0 alone sorts cells of more than 64)
+    }
+}
+
+// One cell of k_cell_sort (one warp): stable ranking by the sort key.
+__device__ __forceinline__ void cell_sort_one(const int* start, int* perm, const int* comp,
+                                              const unsigned char* msub, int c, int lane) {
     int b = start[c], e = start[c + 1], m = e - b;
     if (m <= 1) return;
     if (m <= 64) {
@@ -519,6 +534,8 @@ __global__ void k_cell_sort(const int* start, int ncells, int* perm, const int* 
 // outputs F, M, Vi only with `outputs`.
 __global__ void k_permute(State dst, State src, const int* perm, const int* mcell, const unsigned* need, int outputs) {
     if (!*need) return;
+    // one molecule per thread (a grid-stride loop here let the compiler overlap iterations at 80 registers,
+    // and the gathers ran at a third of the occupancy)
     int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= src.n) return;
     int64_t i = perm[k];
@@ -540,13 +557,13 @@ __global__ void k_permute(State dst, State src, const int* perm, const int* mcel
 __global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, const unsigned* need,
                         float4* xl_other) {
     if (need && !*need) return;
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+#pragma unroll 1
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= S.n; i += (int64_t)gridDim.x * blockDim.x) {
     if (i == S.n) {  // the far-away slot that pads candidate rows (in both local-coordinate buffers)
         xlf[i] = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(0));
         if (xl_other) xl_other[i] = xlf[i];
-        return;
+        continue;
     }
-    if (i > S.n) return;
     int h = S.home[i];
     int cx = h % cP.ln[0], cy = (h / cP.ln[0]) % cP.ln[1], cz = h / (cP.ln[0] * cP.ln[1]);
     double ox = cP.bmin[0] + cx * cP.lside[0], oy = cP.bmin[1] + cy * cP.lside[1], oz = cP.bmin[2] + cz * cP.lside[2];
@@ -558,6 +575,7 @@ __global__ void k_local(State S, float4* xlf, double* origin, float4* xlref, con
     p.w = __int_as_float(S.comp[i]);
     xlf[i] = p;
     xlref[i] = p;
+    }
 }
 
 // Pair-candidate rows of the thread-per-molecule kernels (single-centre LJ)
@@ -796,8 +814,6 @@ __global__ void __launch_bounds__(BL_WARPS * 32, 8) k_build_list(int64_t n, cons
     __shared__ __align__(16) float sq[BL_WARPS][4][32];
     __shared__ uint32_t sbuf[BL_WARPS][32][BL_BUF + 1];  // +1: no bank conflicts between lanes
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c = blockIdx.x * BL_WARPS + wl;
-    if (c >= ncells) return;  // warp-uniform; only warp-level synchronisation below
     ListGrid g;
     for (int d = 0; d < 3; ++d) {
         g.ln[d] = cP.ln[d];
@@ -805,7 +821,11 @@ __global__ void __launch_bounds__(BL_WARPS * 32, 8) k_build_list(int64_t n, cons
         g.per[d] = cP.periodic[d] != 0;
     }
     g.base = 0;
-    build_cell_rows<IL>(n, xl, start, g, c, nbr, nnb, maxnb, rl2, status, need_max, &sq[wl][0][0], sbuf[wl], lane);
+    // warp-stride over the cells (warp-uniform; only warp-level synchronisation below)
+#pragma unroll 1
+    for (int c = blockIdx.x * BL_WARPS + wl; c < ncells; c += gridDim.x * BL_WARPS)
+        build_cell_rows<IL>(n, xl, start, g, c, nbr, nnb, maxnb, rl2, status, need_max, &sq[wl][0][0], sbuf[wl],
+                            lane);
 }
 
 // ------------------------------------------------------------------ site cache
@@ -822,7 +842,7 @@ __global__ void k_sites(State S, Real* sd, Real* se, int stride) {
     double s = rsqrt(w * w + x * x + y * y + z * z);
     w *= s; x *= s; y *= s; z *= s;
     S.qw[i] = w; S.qx[i] = x; S.qy[i] = y; S.qz[i] = z;
-    if (sizeof(Real) == 4) {
+    if constexpr (sizeof(Real) == 4) {
         // FP32 caches: the rotation in FP32 from the normalised FP64 quaternion (rounded on the integer pipes;
         // GB300's FP64 rate made the FP64 rotations most of this kernel's time)
         const float wf = d2f_int(w), xf = d2f_int(x), yf = d2f_int(y), zf = d2f_int(z);
@@ -835,15 +855,15 @@ __global__ void k_sites(State S, Real* sd, Real* se, int stride) {
                 for (int e = 0; e < 3; ++e) se[((int64_t)i * stride + k) * MD_SITE_VEC + e] = (Real)o[e];
             }
         }
-        return;
-    }
-    for (int k = 0; k < C.ns; ++k) {
-        double o[3];
-        qrot(w, x, y, z, C.d[k], o);
-        for (int e = 0; e < 3; ++e) sd[((int64_t)i * stride + k) * MD_SITE_VEC + e] = (Real)o[e];
-        if (C.kind[k] >= SK_DIPOLE) {
-            qrot(w, x, y, z, C.e[k], o);
-            for (int e = 0; e < 3; ++e) se[((int64_t)i * stride + k) * MD_SITE_VEC + e] = (Real)o[e];
+    } else {
+        for (int k = 0; k < C.ns; ++k) {
+            double o[3];
+            qrot(w, x, y, z, C.d[k], o);
+            for (int e = 0; e < 3; ++e) sd[((int64_t)i * stride + k) * MD_SITE_VEC + e] = (Real)o[e];
+            if (C.kind[k] >= SK_DIPOLE) {
+                qrot(w, x, y, z, C.e[k], o);
+                for (int e = 0; e < 3; ++e) se[((int64_t)i * stride + k) * MD_SITE_VEC + e] = (Real)o[e];
+            }
         }
     }
 }
@@ -1390,13 +1410,23 @@ __global__ void __launch_bounds__(256) k_force_lj64(State S, const float4* __res
 // With nhalf (the multi-site kernels' Newton-3 form) each row is first split
 // into the neighbours in higher slots and those in lower slots, each part
 // partitioned by component; nhalf[i] = the length of the first part.
+__device__ __forceinline__ void row_partition_one(const float4* __restrict__ xl, uint32_t* nbr, const int* nnb,
+                                                  int maxnb, int ncomp, int* nhalf, uint32_t* rowbuf, int wl,
+                                                  int lane, int64_t i);
 __global__ void k_row_partition(int64_t n, const float4* __restrict__ xl, uint32_t* nbr, const int* nnb, int maxnb,
                                 int ncomp, const unsigned* need, int* nhalf) {
     if (!*need) return;
     extern __shared__ uint32_t rowbuf[];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + wl;
-    if (i >= n) return;  // warp-uniform
+#pragma unroll 1
+    for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + wl; i < n; i += (int64_t)gridDim.x * (blockDim.x >> 5))
+        row_partition_one(xl, nbr, nnb, maxnb, ncomp, nhalf, rowbuf, wl, lane, i);
+}
+
+// One row of k_row_partition (one warp; its staging areas at rowbuf).
+__device__ __forceinline__ void row_partition_one(const float4* __restrict__ xl, uint32_t* nbr, const int* nnb,
+                                                  int maxnb, int ncomp, int* nhalf, uint32_t* rowbuf, int wl,
+                                                  int lane, int64_t i) {
     uint32_t* buf = rowbuf + (size_t)wl * maxnb;
     // each entry's part (lower half x ncomp + the neighbour's component), found once
     uint8_t* key = reinterpret_cast<uint8_t*>(rowbuf + (size_t)(blockDim.x >> 5) * maxnb) + (size_t)wl * maxnb;
