@@ -141,7 +141,8 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.lines = []
+        self.lines = []      # (time, line) of every sample
+        self.t_end = None
 
     def start(self):
         try:
@@ -155,11 +156,20 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def stop(self) -> dict:
+    def stop(self, wait_s: float = 1.0) -> dict:
+        """Samples taken since start(); when the timed region was shorter than
+        nvidia-smi's start-up and sampling period, waits (up to wait_s) for the
+        first sample, which then describes the clocks right after the region
+        (clock locks and throttle reasons persist); `after_region` counts such
+        samples."""
         if not self.proc:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.t_end = time.perf_counter()
+        deadline = self.t_end + wait_s
+        while not self.lines and time.perf_counter() < deadline:
+            time.sleep(0.01)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -167,7 +177,8 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        after = sum(1 for t, _ in self.lines if t > self.t_end)
+        for _, line in self.lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -180,9 +191,9 @@ class ClockSampler:
                 if f[5 + k].lower().startswith("active"):
                     reasons.add(nm)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "after_region": after}
 
 
 # ---------------------------------------------------------------- CPU baseline (oracle)
@@ -754,6 +765,9 @@ def main():
     sms = cu.attr(16, local)                       # cudaDevAttrMultiProcessorCount
     max_mhz = cu.attr(13, local) / 1e3             # cudaDevAttrClockRate (kHz)
     sm_mhz = clocks.get("sm_mhz") or max_mhz
+    if clocks.get("sm_max_mhz") is None:  # no nvidia-smi sample: the device's own maximum clock
+        clocks["sm_max_mhz"] = max_mhz
+        clocks["sm_max_source"] = "device attribute"
     fp32_peak = sms * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
     fp64_lane_note = "FP64 kernel: bound by GB300's FP64 rate, not FP32" if a.precision == "fp64" else None
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
