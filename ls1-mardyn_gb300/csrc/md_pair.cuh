@@ -81,7 +81,7 @@ __device__ __forceinline__ void cd_body(const Real* d, Real q, const Real* e, Re
 }
 
 // dipole(1)-dipole(2) with reaction field (VCP.cpp:349-442); with T2ON also
-// the torque on dipole 2 (the formula of dd_torque2, from the shared terms)
+// the torque on dipole 2 (VCP.cpp:435-441), from the shared terms
 template <typename Real, bool T2ON = false>
 __device__ __forceinline__ void dd_body(const Real* d, const Real* ei, Real pi, const Real* ej, Real pj, Real epsRF,
                                         Real* f, Real* T1, Real& u, Real& urf, Real* T2 = nullptr) {
@@ -109,22 +109,6 @@ __device__ __forceinline__ void dd_body(const Real* d, const Real* ei, Real pi, 
         Real exd2[3] = {ej[1] * d[2] - ej[2] * d[1], ej[2] * d[0] - ej[0] * d[2], ej[0] * d[1] - ej[1] * d[0]};
         for (int c = 0; c < 3; ++c) T2[c] = p1p2r3 * (re1threeperr2 * exd2[c] + x12[c]) - rffac * x12[c];
     }
-}
-
-// torque on dipole 2 of the dipole-dipole body (VCP.cpp:435-441)
-template <typename Real>
-__device__ __forceinline__ void dd_torque2(const Real* d, const Real* ei, Real pi, const Real* ej, Real pj, Real epsRF,
-                                           Real* T2) {
-    Real r2 = dot3(d, d);
-    Real r2inv = rcp_<Real>(r2);
-    Real rinv = sqrt_<Real>(r2inv);
-    Real p1p2 = pi * pj;
-    Real rffac = p1p2 * epsRF;
-    Real p1p2r3 = p1p2 * rinv * r2inv;
-    Real re1threeperr2 = dot3(d, ei) * ((Real)3 * r2inv);
-    Real x12[3] = {ei[1] * ej[2] - ei[2] * ej[1], ei[2] * ej[0] - ei[0] * ej[2], ei[0] * ej[1] - ei[1] * ej[0]};
-    Real exd[3] = {ej[1] * d[2] - ej[2] * d[1], ej[2] * d[0] - ej[0] * d[2], ej[0] * d[1] - ej[1] * d[0]};
-    for (int c = 0; c < 3; ++c) T2[c] = p1p2r3 * (re1threeperr2 * exd[c] + x12[c]) - rffac * x12[c];
 }
 
 // charge(1)-quadrupole(2) (VCP.cpp:444-524): f on the charge, T on the quadrupole
