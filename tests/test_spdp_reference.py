@@ -6,10 +6,11 @@ periodic DPDP fixtures per_*.npz.
 
 CPU: the reference's SPDP pair counts equal its DPDP ones, and its errors
 against DPDP are those of FP32 pair arithmetic (force rms below 1e-5).
-GPU: on the same inputs the engine's mixed precision is at least as close
-to the reference's DPDP forces and torques as the reference's own SPDP
-build (within a factor 1.5, plus a floor at FP64 rounding level; measured
-1.4-4x closer), and its Upot and virial within 5e-6 relative.  The engine's
+GPU: on the same inputs the engine's mixed precision -- with the rows and
+with the Newton-3 forms -- is at least as close to the reference's DPDP
+forces and torques as the reference's own SPDP build (within a factor 1.5,
+plus a floor at FP64 rounding level; measured 1.4-4x closer with the
+rows), and its Upot and virial within 5e-6 relative.  The engine's
 Upot and virial totals are the less accurate ones (measured 3e-9 to 2e-6
 against the SPDP build's 3e-9 to 3e-6, up to 20x apart on the 4,000-molecule
 box); compensated per-molecule energy and virial sums, a Newton step on the
@@ -54,16 +55,23 @@ def test_reference_spdp_error_against_its_dpdp(case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("scheme", ["rows", "newton3"])
 @pytest.mark.parametrize("case", CASES)
-def test_engine_mixed_at_least_as_close_as_the_reference_spdp(case):
+def test_engine_mixed_at_least_as_close_as_the_reference_spdp(case, scheme):
+    """Both pair schemes: the rows, and the Newton-3 forms (cluster pairs for
+    single-centre LJ with rc_lj = rc, half rows with atomics for the
+    mixture; every one of these boxes has three list cells per axis at skin
+    0, and the case with rc_lj < rc runs on the rows)."""
     import build as eb
     eb.build()
     from ls1gb300 import engine as E
     ps, g, z = _spdp(case)
     ref = _errors(z["F"], z["M"], float(z["upot"]), float(z["virial"]), g)
-    e = E.Engine(ps, g["rc"], g["rc_lj"], precision="mixed")
+    e = E.Engine(ps, g["rc"], g["rc_lj"], precision="mixed", pair_scheme=scheme)
     fo = e.forces()
     m = e.molecules()
+    n3 = scheme == "newton3" and (case == "mix500" or float(g["rc_lj"]) == float(g["rc"]))
+    assert e.time_kernels(1).pair_scheme == (1 if n3 else 0)
     e.close()
     o = np.argsort(m["ids"])
     got = _errors(m["F"][o], m["M"][o], fo.upot, fo.virial, g)
